@@ -1,0 +1,169 @@
+/*
+ * sloth_gpu.h -- C ABI of the GB300 rasterization path for sloth (ecumene/rust-sloth).
+ *
+ * The library replaces the body of sloth's per-frame draw path:
+ *   Context::clear      src/context.rs:35-45
+ *   Context::update     src/context.rs:93-141   (the viewport transform, host math)
+ *   draw_mesh           src/rasterizer.rs:39-46  (-> draw_triangle :48-93, default_shader :5-27)
+ *   frame_buffer/z_buffer read-back (what Context::flush prints, src/context.rs:50-92)
+ * and keeps the reference's results bit for bit: depth cells, frame cells (char and
+ * colour), the newline sentinels of image mode and the draw-order tie-break.
+ *
+ * Conventions
+ *  - Plain C types, caller-owned host buffers, library-owned device buffers.
+ *  - Every fallible call returns sloth_status; sloth_ctx_last_error() gives the text.
+ *    Nothing panics or throws across the ABI.
+ *  - One CUDA stream per context (caller-supplied or library-created); calls on one
+ *    context are not thread-safe, like the reference's &mut Context.
+ *  - Matrices are row-major float[16] (nalgebra's Matrix4::new argument order).
+ *  - A frame cell is a uint32: byte0 = ASCII char, byte1 = r, byte2 = g, byte3 = b.
+ *    The reference's (char,(u8,u8,u8)) cell; all chars it produces are ASCII.
+ *  - The shader is fixed to default_shader (a Rust closure cannot cross a C ABI);
+ *    its thresholds are exported by sloth_shader_thresholds().
+ */
+#ifndef SLOTH_GPU_H
+#define SLOTH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sloth_status {
+    SLOTH_OK = 0,
+    SLOTH_ERR_INVALID_ARGUMENT = 1,
+    SLOTH_ERR_OUT_OF_MEMORY = 2,
+    SLOTH_ERR_CUDA = 3,
+    SLOTH_ERR_LIMIT = 4,          /* a size beyond a documented limit */
+    SLOTH_ERR_DEVICE_FAULT = 5    /* a kernel reported an internal error flag */
+} sloth_status;
+
+typedef struct sloth_ctx sloth_ctx;
+typedef struct sloth_mesh sloth_mesh;
+
+/* Limits of this implementation. */
+#define SLOTH_MAX_DIM 65535u              /* width/height: the reference casts them to u16 in update */
+#define SLOTH_MAX_TRIANGLES 0x7fffffffu   /* triangles drawn between two clears (31-bit draw index) */
+
+/* ---- library ---------------------------------------------------------------------- */
+
+/* Version string of this library. */
+const char *sloth_version(void);
+
+/* default_shader's ramp (src/rasterizer.rs:5-27): thresholds[9] = 0.2f..1.0f and
+ * chars[10] = ".:-=+*#%@ " (the last char is used above 1.0 and for NaN). */
+void sloth_shader_thresholds(float thresholds[9], char chars[10]);
+
+/* default_shader itself, evaluated on the host (src/rasterizer.rs:5-27). */
+char sloth_default_shader(float shade);
+
+/* ---- host math the reference does before drawing ---------------------------------- */
+
+/* nalgebra 0.22.1 Rotation3::from_euler_angles(roll, pitch, yaw).to_homogeneous(),
+ * as built per frame at src/main.rs:76-77.  out: row-major 4x4. */
+void sloth_euler_rotation(float roll, float pitch, float yaw, float out[16]);
+
+/* nalgebra Matrix4 * Matrix4 (src/rasterizer.rs:57 utransform*transform), with its
+ * column-by-column, left-to-right accumulation order. */
+void sloth_mat4_mul(const float a[16], const float b[16], float out[16]);
+
+/* The scene extent of Context::update (src/context.rs:106-113): the fold
+ * 0.0.max(bbox.max.x).max(bbox.max.y).max(bbox.max.z) over meshes.
+ * bbox_max: 3 floats per mesh. */
+float sloth_scene_extent(const float *bbox_max, uint32_t nmesh);
+
+/* The utransform of Context::update (src/context.rs:114-133) for a width x height
+ * context and a scene extent.  out: row-major 4x4. */
+void sloth_viewport_transform(uint16_t width, uint16_t height, float extent, float out[16]);
+
+/* ---- context (src/context.rs:12-49) ------------------------------------------------- */
+
+/* Create a context on CUDA device `device`.  `stream` is a cudaStream_t to issue all
+ * work on, or NULL for a library-owned stream.  The context starts blank like
+ * Context::blank(image=false) (src/context.rs:22-34): 0x0 viewport, identity
+ * utransform. */
+sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream);
+void sloth_ctx_destroy(sloth_ctx *ctx);
+
+/* Text of the last error on this context ("" when none). */
+const char *sloth_ctx_last_error(const sloth_ctx *ctx);
+
+/* Set width, height and image mode (Context{width,height,image}; match_dimensions,
+ * src/inputs.rs:159-169, or the terminal size).  image != 0 gives w*h+h frame cells
+ * with newline sentinels (src/context.rs:36-42, src/rasterizer.rs:89-91).
+ * 1 <= width,height <= SLOTH_MAX_DIM.  Takes effect at the next clear. */
+sloth_status sloth_ctx_set_viewport(sloth_ctx *ctx, uint32_t width, uint32_t height, int image);
+
+/* Set the utransform directly (Context.utransform / Context::camera, src/context.rs:46-49). */
+sloth_status sloth_ctx_set_utransform(sloth_ctx *ctx, const float u[16]);
+
+/* Context::update (src/context.rs:93-141) for image mode: utransform from the meshes'
+ * bounding boxes and the current viewport. */
+sloth_status sloth_ctx_update(sloth_ctx *ctx, const sloth_mesh *const *meshes, uint32_t nmesh);
+
+/* Context::clear (src/context.rs:35-45): depth <- f32::MAX, frame <- (' ',(0,0,0)),
+ * and the draw-order counter restarts. */
+sloth_status sloth_ctx_clear(sloth_ctx *ctx);
+
+/* Number of frame cells (w*h, or w*h+h in image mode) and depth cells (w*h). */
+sloth_status sloth_ctx_sizes(const sloth_ctx *ctx, uint64_t *frame_cells, uint64_t *depth_cells);
+
+/* Copy the frame (Context.frame_buffer) and depth (Context.z_buffer) buffers to host
+ * memory; any argument may be NULL.  `winner` (w*h int32) receives the draw index of
+ * the triangle that last passed the depth test at each depth cell, or -1.
+ * Blocks until the copies complete. */
+sloth_status sloth_ctx_read(sloth_ctx *ctx, uint32_t *cells, float *z, int32_t *winner);
+
+/* Device pointers of the resolved buffers (valid until the next clear/resize/destroy),
+ * for consumers that stay on the GPU.  Resolves pending draws first (asynchronously). */
+sloth_status sloth_ctx_device_buffers(sloth_ctx *ctx, const uint32_t **cells, const float **z);
+
+/* Covered samples (all three edge functions >= 0, src/rasterizer.rs:75) since the last
+ * clear, counted by the raster kernels.  Blocks until pending work completes. */
+sloth_status sloth_ctx_fragments(sloth_ctx *ctx, uint64_t *fragments);
+
+/* ---- meshes (SimpleMesh, src/geometry.rs:78-81) ------------------------------------ */
+
+/* Upload a mesh to the context's device.  x,y,z: nvert vertex positions (structure of
+ * arrays).  idx: 3*ntri vertex indices, or NULL for an unindexed triangle soup
+ * (triangle t uses vertices 3t, 3t+1, 3t+2; then nvert must be 3*ntri).  rgb: 3*ntri
+ * face colours (Triangle.color).  bbox_max: the SimpleMesh bounding_box.max (x,y,z) that
+ * Context::update folds, or NULL to use the loader rule of OBJ meshes
+ * (src/geometry.rs:86-89,128-135: a box grown from the origin). */
+sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, const float *z,
+                               uint32_t nvert, const uint32_t *idx, uint32_t ntri,
+                               const uint8_t *rgb, const float *bbox_max, sloth_mesh **out);
+void sloth_mesh_destroy(sloth_mesh *mesh);
+
+/* Overwrite a mesh's vertex positions and face colours in place (same nvert/ntri), with
+ * asynchronous copies on the context's stream; page-locked host buffers make them true
+ * async copies.  The buffers must stay valid until the next synchronising call. */
+sloth_status sloth_mesh_update(sloth_mesh *mesh, const float *x, const float *y, const float *z,
+                               const uint8_t *rgb);
+sloth_status sloth_mesh_info(const sloth_mesh *mesh, uint32_t *ntri, float bbox_max[3]);
+
+/* ---- the hot path ----------------------------------------------------------------- */
+
+/* draw_mesh(context, mesh, transform, default_shader) (src/rasterizer.rs:39-46): draws
+ * every triangle of `mesh` in order, after all triangles drawn since the last clear.
+ * transform: the row-major rotation (or any model matrix); the library forms
+ * utransform*transform once, in nalgebra's order.  Asynchronous on the ctx stream. */
+sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float transform[16]);
+
+/* ---- timing hooks for benchmarks -------------------------------------------------- */
+
+/* Enable (1) / disable (0) CUDA-event timing of each kernel the context launches.
+ * sloth_ctx_kernel_time() then reports the summed device time (ms) and launch count
+ * of kernel `name` ("setup", "bin_count_large", "bin_scan", "bin_fill", "bin_fill_large",
+ * "raster", "resolve") since timing was enabled; blocks until the events complete. */
+sloth_status sloth_ctx_set_timing(sloth_ctx *ctx, int enable);
+sloth_status sloth_ctx_kernel_time(sloth_ctx *ctx, const char *name, double *ms, uint64_t *launches);
+/* Number of kernels launched by this context since creation. */
+uint64_t sloth_ctx_launch_count(const sloth_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

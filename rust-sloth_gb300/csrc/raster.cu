@@ -1,0 +1,125 @@
+// raster.cu -- per-tile rasterization with a shared-memory depth-key tile.
+//
+// Replaces the sample loop of src/rasterizer.rs:69-86.  One CTA owns one tile of depth
+// cells (kTileH rows x kTileW cells).  Its warps take the tile's triangle entries one at
+// a time; the 32 lanes walk the triangle's samples inside the tile (unwrapped and wrapped
+// parts), evaluate the three edge functions and the barycentric depth in the reference's
+// f32 operation order, and fold (depth, draw index) keys into the tile with a 64-bit
+// shared-memory atomicMin.  The minimum key of a cell is the reference's last successful
+// depth write.  Keys of earlier draws since the clear are merged in first.
+#include "sloth_internal.cuh"
+#include "sloth_kernels.h"
+
+namespace sloth {
+
+constexpr int TW = kTileW, TH = kTileH;
+
+__device__ __forceinline__ TriRecord load_record(const TriRecord *__restrict__ recs, uint32_t i)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(recs + i);
+    TriRecord r;
+    float4 *o = reinterpret_cast<float4 *>(&r);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[k] = __ldg(p + k);
+    return r;
+}
+
+// Walk the samples of rect c (row-major, 32 at a time) and fold covered samples' keys.
+template <int kNotWrapped>
+__device__ __forceinline__ void raster_part(const TriRecord &r, uint32_t gtri, Rect c, int R0,
+                                            int C0, int w, unsigned long long *skeys, int lane,
+                                            uint32_t &frags)
+{
+    if (c.empty()) return;
+    if ((r.flags & kFlagFiniteXY) && !rect_may_cover(r, c)) return;
+    const int bw = c.xb - c.xa;
+    const int area = bw * (c.yb - c.ya);
+    const int q = 32 / bw, rem = 32 - q * bw;
+    int dx = lane % bw, dy = lane / bw;
+    for (int k = lane; k < area; k += 32) {
+        const int x = c.xa + dx, y = c.ya + dy;
+        const float px = (float)x, py = (float)y;
+        const EdgeVals e = eval_edges(r, px, py);
+        if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
+            ++frags;
+            const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
+            if (z < kFltMax) {
+                const unsigned long long key = make_key(z, gtri, kNotWrapped);
+                const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
+                const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
+                unsigned long long *p = &skeys[row * TW + col];
+                if (key < *(volatile unsigned long long *)p) atomicMin(p, key);
+            }
+        }
+        dx += rem;
+        dy += q;
+        if (dx >= bw) {
+            dx -= bw;
+            ++dy;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256)
+raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb)
+{
+    __shared__ unsigned long long skeys[TH * TW];
+    __shared__ uint32_t s_next;
+    __shared__ uint32_t s_frags[8];
+    const int tile = blockIdx.x;
+    const uint32_t cnt = bb.tile_count[tile];
+    if (cnt == 0) return;
+    const uint32_t off = bb.tile_offset[tile];
+    const int tr = tile / g.ntx, tc = tile - (tile / g.ntx) * g.ntx;
+    const int R0 = tr * TH, C0 = tc * TW;
+    const bool merge = fb.tile_gen[tile] == fb.gen;
+    unsigned long long *gk = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)R0 * g.pitch + C0;
+    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+        const int rr = i / TW, cc = i - rr * TW;
+        skeys[i] = merge ? gk[(size_t)rr * g.pitch + cc] : kEmptyKey;
+    }
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const Viewport vp{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
+    uint32_t frags = 0;
+    for (;;) {
+        uint32_t e = 0;
+        if (lane == 0) e = atomicAdd(&s_next, 1u);
+        e = __shfl_sync(0xffffffffu, e, 0);
+        if (e >= cnt) break;
+        const uint32_t gtri = __ldg(bb.entries + off + e);
+        const TriRecord r = load_record(fb.records, gtri);
+        const Rect U = unwrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
+        if (!U.empty()) raster_part<1>(r, gtri, clip_unwrapped(vp, U, tr, tc), R0, C0, g.w, skeys, lane, frags);
+        const Rect W = wrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
+        if (!W.empty()) raster_part<0>(r, gtri, clip_wrapped(vp, W, tr, tc), R0, C0, g.w, skeys, lane, frags);
+    }
+    // fragment count: warp reduce, then one atomic per CTA
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) frags += __shfl_xor_sync(0xffffffffu, frags, d);
+    if (lane == 0) s_frags[threadIdx.x >> 5] = frags;
+    __syncthreads();
+    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+        const int rr = i / TW, cc = i - rr * TW;
+        gk[(size_t)rr * g.pitch + cc] = skeys[i];
+    }
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) tot += s_frags[k];
+        atomicAdd(fb.fragments, (unsigned long long)tot);
+        fb.tile_gen[tile] = fb.gen;
+    }
+}
+
+cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
+                          cudaStream_t s)
+{
+    const int ntiles = g.ntx * g.nty;
+    if (ntiles == 0) return cudaSuccess;
+    raster_kernel<<<ntiles, 256, 0, s>>>(g, fb, bb);
+    return cudaGetLastError();
+}
+
+}  // namespace sloth

@@ -1,0 +1,660 @@
+// sloth_api.cpp -- the C ABI (include/sloth_gpu.h): contexts, meshes and the draw path.
+//
+// Host-side restatement of the reference's per-frame driver around the hot path:
+// Context::blank/update/clear (src/context.rs:22-45, 93-141), draw_mesh
+// (src/rasterizer.rs:39-46) and the buffer reads that Context::flush prints.  All device
+// memory is owned here; all work is issued on the context's stream.  There is no CPU
+// fallback: if CUDA or the kernels are unavailable every call fails with SLOTH_ERR_CUDA.
+//
+// Host float math below must be compiled with -ffp-contract=off (see build.py).
+#include "sloth_gpu.h"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sloth_internal.cuh"
+#include "sloth_kernels.h"
+
+using namespace sloth;
+
+namespace {
+
+struct EventPair {
+    cudaEvent_t a, b;
+};
+struct KernelClock {
+    double ms = 0.0;
+    uint64_t launches = 0;
+    std::vector<EventPair> pending;
+};
+
+}  // namespace
+
+struct sloth_mesh {
+    sloth_ctx *ctx = nullptr;
+    int device = 0;
+    float *x = nullptr, *y = nullptr, *z = nullptr;
+    uint32_t *idx = nullptr;
+    uint8_t *rgb = nullptr;
+    uint32_t nvert = 0, ntri = 0;
+    float bbox_max[3] = {0, 0, 0};
+};
+
+struct sloth_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+
+    // requested viewport (Context.width/height/image) and utransform
+    uint32_t req_w = 0, req_h = 0;
+    int req_image = 0;
+    float U[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+
+    // allocated frame state
+    bool have_frame = false;
+    FrameGeom g{};
+    FrameBuffers fb{};
+    size_t records_cap = 0;
+    BinBuffers bb{};
+    uint32_t ntiles_cap = 0;
+    size_t large_cap = 0;
+    float4 *tv = nullptr;
+    size_t tv_cap = 0;
+    uint32_t *h_total = nullptr;   // pinned
+    unsigned long long *h_frags = nullptr;   // pinned
+    uint32_t tri_base = 0;
+    bool dirty = true;
+
+    // instrumentation
+    bool timing = false;
+    std::map<std::string, KernelClock> clocks;
+    uint64_t launches = 0;
+};
+
+// ---------------------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------------------
+static sloth_status fail(sloth_ctx *ctx, sloth_status st, const char *fmt, ...)
+{
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return st;
+}
+
+#define CU(ctx, call)                                                                   \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return fail((ctx), e_ == cudaErrorMemoryAllocation ? SLOTH_ERR_OUT_OF_MEMORY \
+                                                               : SLOTH_ERR_CUDA,        \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                \
+    } while (0)
+
+template <class T>
+static cudaError_t dalloc(T **p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T));
+}
+
+template <class T>
+static void dfree(T *&p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// Time one launch on the ctx stream when timing is enabled.
+template <class F>
+static cudaError_t timed(sloth_ctx *ctx, const char *name, F &&launch)
+{
+    if (!ctx->timing) {
+        cudaError_t e = launch();
+        if (e == cudaSuccess) ctx->launches++;
+        return e;
+    }
+    EventPair ev;
+    cudaEventCreate(&ev.a);
+    cudaEventCreate(&ev.b);
+    cudaEventRecord(ev.a, ctx->stream);
+    cudaError_t e = launch();
+    cudaEventRecord(ev.b, ctx->stream);
+    if (e == cudaSuccess) {
+        ctx->launches++;
+        ctx->clocks[name].pending.push_back(ev);
+    } else {
+        cudaEventDestroy(ev.a);
+        cudaEventDestroy(ev.b);
+    }
+    return e;
+}
+
+static void free_frame(sloth_ctx *ctx)
+{
+    dfree(ctx->fb.keys);
+    dfree(ctx->fb.tile_gen);
+    dfree(ctx->fb.rownl);
+    dfree(ctx->fb.z_out);
+    dfree(ctx->fb.cells_out);
+    dfree(ctx->fb.winner_out);
+    dfree(ctx->fb.fragments);
+    dfree(ctx->bb.tile_count);
+    dfree(ctx->bb.tile_offset);
+    dfree(ctx->bb.tile_cursor);
+    ctx->have_frame = false;
+    ctx->ntiles_cap = 0;
+}
+
+// (Re)allocate the per-frame buffers for the requested viewport.
+static sloth_status alloc_frame(sloth_ctx *ctx)
+{
+    free_frame(ctx);
+    FrameGeom g{};
+    g.w = (int32_t)ctx->req_w;
+    g.h = (int32_t)ctx->req_h;
+    g.image = ctx->req_image ? 1 : 0;
+    g.tw = kTileW;
+    g.th = kTileH;
+    g.ntx = (g.w + g.tw - 1) / g.tw;
+    g.nty = (g.h + g.th - 1) / g.th;
+    g.pitch = g.ntx * g.tw;
+    const size_t ntiles = (size_t)g.ntx * g.nty;
+    const size_t nz = (size_t)g.w * g.h;
+    const size_t ncells = g.image ? nz + g.h : nz;
+    CU(ctx, dalloc(&ctx->fb.keys, (size_t)g.pitch * g.nty * g.th));
+    CU(ctx, dalloc(&ctx->fb.tile_gen, ntiles));
+    CU(ctx, cudaMemsetAsync(ctx->fb.tile_gen, 0, ntiles * sizeof(uint32_t), ctx->stream));
+    CU(ctx, dalloc(&ctx->fb.rownl, (size_t)g.h));
+    CU(ctx, dalloc(&ctx->fb.z_out, nz));
+    CU(ctx, dalloc(&ctx->fb.cells_out, ncells));
+    CU(ctx, dalloc(&ctx->fb.winner_out, nz));
+    CU(ctx, dalloc(&ctx->fb.fragments, 1));
+    CU(ctx, dalloc(&ctx->bb.tile_count, ntiles));
+    CU(ctx, dalloc(&ctx->bb.tile_offset, ntiles + 1));
+    CU(ctx, dalloc(&ctx->bb.tile_cursor, ntiles));
+    ctx->ntiles_cap = (uint32_t)ntiles;
+    ctx->fb.gen = 0;
+    ctx->g = g;
+    ctx->have_frame = true;
+    return SLOTH_OK;
+}
+
+static sloth_status ensure_records(sloth_ctx *ctx, size_t need)
+{
+    if (need <= ctx->records_cap) return SLOTH_OK;
+    size_t cap = ctx->records_cap ? ctx->records_cap : 1024;
+    while (cap < need) cap *= 2;
+    TriRecord *n = nullptr;
+    CU(ctx, dalloc(&n, cap));
+    if (ctx->fb.records && ctx->tri_base)
+        CU(ctx, cudaMemcpyAsync(n, ctx->fb.records, (size_t)ctx->tri_base * sizeof(TriRecord),
+                                cudaMemcpyDeviceToDevice, ctx->stream));
+    CU(ctx, cudaStreamSynchronize(ctx->stream));
+    dfree(ctx->fb.records);
+    ctx->fb.records = n;
+    ctx->records_cap = cap;
+    return SLOTH_OK;
+}
+
+template <class T>
+static sloth_status ensure_scratch(sloth_ctx *ctx, T **p, size_t *cap, size_t need)
+{
+    if (need <= *cap && *p) return SLOTH_OK;
+    size_t c = *cap ? *cap : 1024;
+    while (c < need) c *= 2;
+    CU(ctx, cudaStreamSynchronize(ctx->stream));
+    dfree(*p);
+    CU(ctx, dalloc(p, c));
+    *cap = c;
+    return SLOTH_OK;
+}
+
+static sloth_status resolve_pending(sloth_ctx *ctx)
+{
+    if (!ctx->have_frame)
+        return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "the context has no frame: call sloth_ctx_clear first");
+    if (!ctx->dirty) return SLOTH_OK;
+    CU(ctx, timed(ctx, "resolve", [&] { return launch_resolve(ctx->g, ctx->fb, ctx->stream); }));
+    ctx->dirty = false;
+    return SLOTH_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// host math (restated from the reference and nalgebra 0.22.1; -ffp-contract=off)
+// ---------------------------------------------------------------------------------------
+extern "C" {
+
+const char *sloth_version(void) { return "sloth-gb300 0.1 (sm_103a)"; }
+
+void sloth_shader_thresholds(float thresholds[9], char chars[10])
+{
+    static const float t[9] = {0.20f, 0.30f, 0.40f, 0.50f, 0.60f, 0.70f, 0.80f, 0.90f, 1.0f};
+    static const char c[10] = {'.', ':', '-', '=', '+', '*', '#', '%', '@', ' '};
+    if (thresholds) memcpy(thresholds, t, sizeof t);
+    if (chars) memcpy(chars, c, sizeof c);
+}
+
+// src/rasterizer.rs:5-27
+char sloth_default_shader(float shade)
+{
+    if (shade <= 0.20f) return '.';
+    if (shade <= 0.30f) return ':';
+    if (shade <= 0.40f) return '-';
+    if (shade <= 0.50f) return '=';
+    if (shade <= 0.60f) return '+';
+    if (shade <= 0.70f) return '*';
+    if (shade <= 0.80f) return '#';
+    if (shade <= 0.90f) return '%';
+    if (shade <= 1.0f) return '@';
+    return ' ';
+}
+
+// nalgebra Rotation3::from_euler_angles (ZYX) + to_homogeneous, src/main.rs:76-77.
+void sloth_euler_rotation(float roll, float pitch, float yaw, float out[16])
+{
+    const float sr = std::sin(roll), cr = std::cos(roll);
+    const float sp = std::sin(pitch), cp = std::cos(pitch);
+    const float sy = std::sin(yaw), cy = std::cos(yaw);
+    const float m[16] = {
+        cy * cp, cy * sp * sr - sy * cr, cy * sp * cr + sy * sr, 0.0f,
+        sy * cp, sy * sp * sr + cy * cr, sy * sp * cr - cy * sr, 0.0f,
+        -sp,     cp * sr,                cp * cr,                0.0f,
+        0.0f,    0.0f,                   0.0f,                   1.0f,
+    };
+    memcpy(out, m, sizeof m);
+}
+
+// nalgebra gemm -> gemv: column by column, first product then + each later product.
+void sloth_mat4_mul(const float a[16], const float b[16], float out[16])
+{
+    float r[16];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            float acc = a[i * 4 + 0] * b[0 * 4 + j];
+            for (int k = 1; k < 4; ++k) acc = a[i * 4 + k] * b[k * 4 + j] + acc;
+            r[i * 4 + j] = acc;
+        }
+    memcpy(out, r, sizeof r);
+}
+
+// src/context.rs:106-113
+float sloth_scene_extent(const float *bbox_max, uint32_t nmesh)
+{
+    float s = 0.0f;
+    for (uint32_t m = 0; m < nmesh; ++m)
+        for (int k = 0; k < 3; ++k) s = std::fmax(s, bbox_max[3 * m + k]);
+    return s;
+}
+
+// src/context.rs:114-133
+void sloth_viewport_transform(uint16_t width, uint16_t height, float extent, float out[16])
+{
+    const float fw = (float)width, fh = (float)height;
+    const float scale = std::fmin(fh, fw / 2.0f) / extent / 2.0f;
+    const float t[16] = {scale, 0.0f,   0.0f,  fw / 4.0f, 0.0f, -scale, 0.0f, fh / 2.0f,
+                         0.0f,  0.0f,   scale, 0.0f,      0.0f, 0.0f,   0.0f, 1.0f};
+    memcpy(out, t, sizeof t);
+}
+
+// ---------------------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------------------
+sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
+{
+    if (!out) return SLOTH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SLOTH_ERR_CUDA;
+    if (device < 0 || device >= ndev) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(device) != cudaSuccess) return SLOTH_ERR_CUDA;
+    sloth_ctx *ctx = new sloth_ctx();
+    ctx->device = device;
+    if (stream) {
+        ctx->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete ctx;
+            return SLOTH_ERR_CUDA;
+        }
+        ctx->own_stream = true;
+    }
+    if (cudaMallocHost(&ctx->h_total, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_frags, sizeof(unsigned long long)) != cudaSuccess) {
+        if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return SLOTH_ERR_OUT_OF_MEMORY;
+    }
+    *out = ctx;
+    return SLOTH_OK;
+}
+
+void sloth_ctx_destroy(sloth_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->clocks)
+        for (auto &ev : kv.second.pending) {
+            cudaEventDestroy(ev.a);
+            cudaEventDestroy(ev.b);
+        }
+    free_frame(ctx);
+    dfree(ctx->fb.records);
+    dfree(ctx->bb.entries);
+    dfree(ctx->bb.large_queue);
+    dfree(ctx->bb.large_count);
+    dfree(ctx->tv);
+    if (ctx->h_total) cudaFreeHost(ctx->h_total);
+    if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *sloth_ctx_last_error(const sloth_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+sloth_status sloth_ctx_set_viewport(sloth_ctx *ctx, uint32_t width, uint32_t height, int image)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (width < 1 || height < 1 || width > SLOTH_MAX_DIM || height > SLOTH_MAX_DIM)
+        return fail(ctx, SLOTH_ERR_LIMIT, "viewport %ux%u outside 1..%u", width, height, SLOTH_MAX_DIM);
+    ctx->req_w = width;
+    ctx->req_h = height;
+    ctx->req_image = image ? 1 : 0;
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_set_utransform(sloth_ctx *ctx, const float u[16])
+{
+    if (!ctx || !u) return SLOTH_ERR_INVALID_ARGUMENT;
+    memcpy(ctx->U, u, sizeof ctx->U);
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_update(sloth_ctx *ctx, const sloth_mesh *const *meshes, uint32_t nmesh)
+{
+    if (!ctx || (nmesh && !meshes)) return SLOTH_ERR_INVALID_ARGUMENT;
+    std::vector<float> bb(3 * (size_t)nmesh);
+    for (uint32_t i = 0; i < nmesh; ++i) {
+        if (!meshes[i]) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "mesh %u is NULL", i);
+        memcpy(&bb[3 * (size_t)i], meshes[i]->bbox_max, 3 * sizeof(float));
+    }
+    const float ext = sloth_scene_extent(bb.data(), nmesh);
+    sloth_viewport_transform((uint16_t)ctx->req_w, (uint16_t)ctx->req_h, ext, ctx->U);
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_clear(sloth_ctx *ctx)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (ctx->req_w == 0 || ctx->req_h == 0)
+        return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "no viewport: call sloth_ctx_set_viewport first");
+    CU(ctx, cudaSetDevice(ctx->device));
+    if (!ctx->have_frame || ctx->g.w != (int32_t)ctx->req_w || ctx->g.h != (int32_t)ctx->req_h ||
+        ctx->g.image != ctx->req_image) {
+        sloth_status st = alloc_frame(ctx);
+        if (st != SLOTH_OK) return st;
+    }
+    // A new generation invalidates every tile's keys without touching them.
+    ctx->fb.gen++;
+    if (ctx->fb.gen == 0) {
+        CU(ctx, cudaMemsetAsync(ctx->fb.tile_gen, 0, ctx->ntiles_cap * sizeof(uint32_t), ctx->stream));
+        ctx->fb.gen = 1;
+    }
+    CU(ctx, cudaMemsetAsync(ctx->fb.rownl, 0xff, (size_t)ctx->g.h * sizeof(int32_t), ctx->stream));
+    CU(ctx, cudaMemsetAsync(ctx->fb.fragments, 0, sizeof(unsigned long long), ctx->stream));
+    ctx->tri_base = 0;
+    ctx->dirty = true;
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_sizes(const sloth_ctx *ctx, uint64_t *frame_cells, uint64_t *depth_cells)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    const uint64_t nz = (uint64_t)ctx->req_w * ctx->req_h;
+    if (frame_cells) *frame_cells = ctx->req_image ? nz + ctx->req_h : nz;
+    if (depth_cells) *depth_cells = nz;
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_read(sloth_ctx *ctx, uint32_t *cells, float *z, int32_t *winner)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    CU(ctx, cudaSetDevice(ctx->device));
+    sloth_status st = resolve_pending(ctx);
+    if (st != SLOTH_OK) return st;
+    const size_t nz = (size_t)ctx->g.w * ctx->g.h;
+    const size_t ncells = ctx->g.image ? nz + ctx->g.h : nz;
+    if (cells)
+        CU(ctx, cudaMemcpyAsync(cells, ctx->fb.cells_out, ncells * sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+    if (z)
+        CU(ctx, cudaMemcpyAsync(z, ctx->fb.z_out, nz * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    if (winner)
+        CU(ctx, cudaMemcpyAsync(winner, ctx->fb.winner_out, nz * sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+    CU(ctx, cudaStreamSynchronize(ctx->stream));
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_device_buffers(sloth_ctx *ctx, const uint32_t **cells, const float **z)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    CU(ctx, cudaSetDevice(ctx->device));
+    sloth_status st = resolve_pending(ctx);
+    if (st != SLOTH_OK) return st;
+    if (cells) *cells = ctx->fb.cells_out;
+    if (z) *z = ctx->fb.z_out;
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_fragments(sloth_ctx *ctx, uint64_t *fragments)
+{
+    if (!ctx || !fragments) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!ctx->have_frame) {
+        *fragments = 0;
+        return SLOTH_OK;
+    }
+    CU(ctx, cudaSetDevice(ctx->device));
+    CU(ctx, cudaMemcpyAsync(ctx->h_frags, ctx->fb.fragments, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    CU(ctx, cudaStreamSynchronize(ctx->stream));
+    *fragments = *ctx->h_frags;
+    return SLOTH_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// meshes
+// ---------------------------------------------------------------------------------------
+sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, const float *z,
+                               uint32_t nvert, const uint32_t *idx, uint32_t ntri,
+                               const uint8_t *rgb, const float *bbox_max, sloth_mesh **out)
+{
+    if (!ctx || !out) return SLOTH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (nvert && (!x || !y || !z)) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "vertex arrays are NULL");
+    if (ntri && !rgb) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "rgb is NULL");
+    if (!idx && (uint64_t)nvert != 3ull * ntri)
+        return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "an unindexed soup needs nvert == 3*ntri (%u vs %u)",
+                    nvert, ntri);
+    if (ntri > SLOTH_MAX_TRIANGLES) return fail(ctx, SLOTH_ERR_LIMIT, "too many triangles");
+    if (idx)
+        for (uint64_t i = 0; i < 3ull * ntri; ++i)
+            if (idx[i] >= nvert)
+                return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "index %u at %llu is out of range (nvert %u)",
+                            idx[i], (unsigned long long)i, nvert);
+    CU(ctx, cudaSetDevice(ctx->device));
+    sloth_mesh *m = new sloth_mesh();
+    m->ctx = ctx;
+    m->device = ctx->device;
+    m->nvert = nvert;
+    m->ntri = ntri;
+    auto cleanup = [&](sloth_status st) {
+        sloth_mesh_destroy(m);
+        return st;
+    };
+    if (dalloc(&m->x, nvert) || dalloc(&m->y, nvert) || dalloc(&m->z, nvert) ||
+        dalloc(&m->rgb, 3 * (size_t)ntri) || (idx && dalloc(&m->idx, 3 * (size_t)ntri)))
+        return cleanup(fail(ctx, SLOTH_ERR_OUT_OF_MEMORY, "mesh allocation failed"));
+    cudaError_t e = cudaSuccess;
+    if (nvert) {
+        e = cudaMemcpy(m->x, x, nvert * sizeof(float), cudaMemcpyHostToDevice);
+        if (!e) e = cudaMemcpy(m->y, y, nvert * sizeof(float), cudaMemcpyHostToDevice);
+        if (!e) e = cudaMemcpy(m->z, z, nvert * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    if (!e && ntri) e = cudaMemcpy(m->rgb, rgb, 3 * (size_t)ntri, cudaMemcpyHostToDevice);
+    if (!e && idx && ntri) e = cudaMemcpy(m->idx, idx, 3 * (size_t)ntri * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e) return cleanup(fail(ctx, SLOTH_ERR_CUDA, "mesh upload failed: %s", cudaGetErrorString(e)));
+    if (bbox_max) {
+        memcpy(m->bbox_max, bbox_max, sizeof m->bbox_max);
+    } else {
+        // OBJ loader rule (src/geometry.rs:86-89,128-135): a box grown from the origin over
+        // every triangle's vertices.
+        float b[3] = {0.0f, 0.0f, 0.0f};
+        const float *xyz[3] = {x, y, z};
+        for (uint64_t t = 0; t < ntri; ++t)
+            for (int k = 0; k < 3; ++k) {
+                const uint64_t vi = idx ? idx[3 * t + k] : 3 * t + k;
+                for (int c = 0; c < 3; ++c) b[c] = std::fmax(xyz[c][vi], b[c]);
+            }
+        memcpy(m->bbox_max, b, sizeof b);
+    }
+    *out = m;
+    return SLOTH_OK;
+}
+
+void sloth_mesh_destroy(sloth_mesh *m)
+{
+    if (!m) return;
+    cudaSetDevice(m->device);
+    dfree(m->x);
+    dfree(m->y);
+    dfree(m->z);
+    dfree(m->idx);
+    dfree(m->rgb);
+    delete m;
+}
+
+sloth_status sloth_mesh_update(sloth_mesh *m, const float *x, const float *y, const float *z,
+                               const uint8_t *rgb)
+{
+    if (!m || !m->ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    sloth_ctx *ctx = m->ctx;
+    if (m->nvert && (!x || !y || !z)) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "vertex arrays are NULL");
+    if (m->ntri && !rgb) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "rgb is NULL");
+    CU(ctx, cudaSetDevice(m->device));
+    const size_t nb = (size_t)m->nvert * sizeof(float);
+    if (m->nvert) {
+        CU(ctx, cudaMemcpyAsync(m->x, x, nb, cudaMemcpyHostToDevice, ctx->stream));
+        CU(ctx, cudaMemcpyAsync(m->y, y, nb, cudaMemcpyHostToDevice, ctx->stream));
+        CU(ctx, cudaMemcpyAsync(m->z, z, nb, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if (m->ntri) CU(ctx, cudaMemcpyAsync(m->rgb, rgb, 3 * (size_t)m->ntri, cudaMemcpyHostToDevice, ctx->stream));
+    return SLOTH_OK;
+}
+
+sloth_status sloth_mesh_info(const sloth_mesh *m, uint32_t *ntri, float bbox_max[3])
+{
+    if (!m) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (ntri) *ntri = m->ntri;
+    if (bbox_max) memcpy(bbox_max, m->bbox_max, sizeof m->bbox_max);
+    return SLOTH_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// draw_mesh
+// ---------------------------------------------------------------------------------------
+sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float transform[16])
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!mesh || !transform) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "mesh or transform is NULL");
+    if (mesh->device != ctx->device) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "mesh is on another device");
+    if (!ctx->have_frame) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "call sloth_ctx_clear before drawing");
+    if (mesh->ntri == 0) return SLOTH_OK;
+    if ((uint64_t)ctx->tri_base + mesh->ntri > SLOTH_MAX_TRIANGLES)
+        return fail(ctx, SLOTH_ERR_LIMIT, "more than %u triangles since the last clear", SLOTH_MAX_TRIANGLES);
+    CU(ctx, cudaSetDevice(ctx->device));
+    sloth_status st;
+    if ((st = ensure_records(ctx, (size_t)ctx->tri_base + mesh->ntri)) != SLOTH_OK) return st;
+    if ((st = ensure_scratch(ctx, &ctx->tv, &ctx->tv_cap, mesh->nvert)) != SLOTH_OK) return st;
+    if ((st = ensure_scratch(ctx, &ctx->bb.large_queue, &ctx->large_cap, mesh->ntri)) != SLOTH_OK) return st;
+    if (!ctx->bb.large_count) CU(ctx, dalloc(&ctx->bb.large_count, 1));
+
+    Mat4 M;
+    sloth_mat4_mul(ctx->U, transform, M.m);
+    MeshDev md{mesh->x, mesh->y, mesh->z, mesh->idx, mesh->rgb, mesh->nvert, mesh->ntri};
+    const FrameGeom &g = ctx->g;
+    const uint32_t ntiles = (uint32_t)(g.ntx * g.nty);
+    cudaStream_t s = ctx->stream;
+    CU(ctx, cudaMemsetAsync(ctx->bb.tile_count, 0, ntiles * sizeof(uint32_t), s));
+    CU(ctx, cudaMemsetAsync(ctx->bb.large_count, 0, sizeof(uint32_t), s));
+    CU(ctx, timed(ctx, "vertex", [&] { return launch_vertex_transform(md, M, ctx->tv, s); }));
+    CU(ctx, timed(ctx, "setup", [&] { return launch_setup(md, ctx->tv, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+    CU(ctx, timed(ctx, "bin_count_large", [&] { return launch_bin_count_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+    CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
+    CU(ctx, cudaMemcpyAsync(ctx->h_total, ctx->bb.tile_offset + ntiles, sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, s));
+    CU(ctx, cudaStreamSynchronize(s));
+    const uint32_t total = *ctx->h_total;
+    size_t ecap = ctx->bb.capacity;
+    if ((st = ensure_scratch(ctx, &ctx->bb.entries, &ecap, total)) != SLOTH_OK) return st;
+    ctx->bb.capacity = (uint32_t)(ecap > 0xffffffffu ? 0xffffffffu : ecap);
+    CU(ctx, timed(ctx, "bin_fill", [&] { return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+    CU(ctx, timed(ctx, "bin_fill_large", [&] { return launch_bin_fill_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+    CU(ctx, timed(ctx, "raster", [&] { return launch_raster(g, ctx->fb, ctx->bb, s); }));
+    ctx->tri_base += mesh->ntri;
+    ctx->dirty = true;
+    return SLOTH_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// timing hooks
+// ---------------------------------------------------------------------------------------
+sloth_status sloth_ctx_set_timing(sloth_ctx *ctx, int enable)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    ctx->timing = enable != 0;
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_kernel_time(sloth_ctx *ctx, const char *name, double *ms, uint64_t *launches)
+{
+    if (!ctx || !name) return SLOTH_ERR_INVALID_ARGUMENT;
+    CU(ctx, cudaSetDevice(ctx->device));
+    auto it = ctx->clocks.find(name);
+    if (it == ctx->clocks.end()) {
+        if (ms) *ms = 0.0;
+        if (launches) *launches = 0;
+        return SLOTH_OK;
+    }
+    KernelClock &kc = it->second;
+    for (auto &ev : kc.pending) {
+        CU(ctx, cudaEventSynchronize(ev.b));
+        float t = 0.0f;
+        CU(ctx, cudaEventElapsedTime(&t, ev.a, ev.b));
+        kc.ms += t;
+        kc.launches++;
+        cudaEventDestroy(ev.a);
+        cudaEventDestroy(ev.b);
+    }
+    kc.pending.clear();
+    if (ms) *ms = kc.ms;
+    if (launches) *launches = kc.launches;
+    return SLOTH_OK;
+}
+
+uint64_t sloth_ctx_launch_count(const sloth_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+}  // extern "C"

