@@ -222,10 +222,15 @@ def run_gpu(args):
         ctx.draw_mesh(dm, R)
         ctx.device_buffers()   # resolve
 
+    # covered samples of one frame (every covered sample counted: depth culling off)
+    ctx.set_depth_cull(False)
+    step()
+    frags = ctx.fragments()
+    ctx.set_depth_cull(not args.no_depth_cull)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    frags = ctx.fragments()
+    frags_evaluated = ctx.fragments()
 
     # ---- device-resident timed region
     ctx.set_timing(True)
@@ -251,7 +256,7 @@ def run_gpu(args):
     launches = ctx.launch_count() - launches0
     ms = sum(a.elapsed_time(b) for a, b in evs)
     kernels = {}
-    for name in ("vertex", "setup", "bin_count_large", "bin_scan", "bin_fill", "bin_fill_large", "raster", "resolve"):
+    for name in ("vertex", "setup", "newline", "bin_count_large", "bin_scan", "bin_fill", "bin_fill_large", "raster", "resolve"):
         t, n = ctx.kernel_time(name)
         if n:
             kernels[name] = {"ms_per_launch": t / n, "launches": n}
@@ -325,6 +330,8 @@ def run_gpu(args):
                    "rotation": "from_euler_angles(0, pi, 0) (CLI default)", "seed": SEED,
                    "l2": "flushed before every timed step (512 MiB write)", "parallelism": f"replicas x{ws}"},
         "gfrag_per_s": frags * value / 1e9, "fragments_per_frame": frags,
+        "fragments_rasterized_per_frame": frags_evaluated,
+        "depth_cull": not args.no_depth_cull,
         "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches, "kernels": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
     }
@@ -341,9 +348,11 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-sample-den", type=int, default=64)
+    ap.add_argument("--cpu-sample-den", type=int, default=8)
     ap.add_argument("--ref-sample-den", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-depth-cull", action="store_true",
+                    help="rasterize every triangle (SLOTH_OPTION_DEPTH_CULL 0)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

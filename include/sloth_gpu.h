@@ -121,8 +121,16 @@ sloth_status sloth_ctx_read(sloth_ctx *ctx, uint32_t *cells, float *z, int32_t *
 sloth_status sloth_ctx_device_buffers(sloth_ctx *ctx, const uint32_t **cells, const float **z);
 
 /* Covered samples (all three edge functions >= 0, src/rasterizer.rs:75) since the last
- * clear, counted by the raster kernels.  Blocks until pending work completes. */
+ * clear, counted by the raster kernels over the triangles they evaluated: every covered
+ * sample when SLOTH_OPTION_DEPTH_CULL is 0.  Blocks until pending work completes. */
 sloth_status sloth_ctx_fragments(sloth_ctx *ctx, uint64_t *fragments);
+
+/* Options (sloth_ctx_set_option).
+ * SLOTH_OPTION_DEPTH_CULL: 1 (default) lets the raster skip triangles proven to lie
+ *   behind every depth cell they could write (a proven depth bound against the tile's
+ *   current depths); 0 rasterizes every triangle.  Results are identical either way. */
+#define SLOTH_OPTION_DEPTH_CULL 1
+sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value);
 
 /* ---- meshes (SimpleMesh, src/geometry.rs:78-81) ------------------------------------ */
 

@@ -97,7 +97,10 @@ __global__ void __launch_bounds__(256) resolve_kernel(FrameGeom g, FrameBuffers 
             if (g.image && (c - 1) % g.w == 0) {
                 const uint64_t yn = (c - 1) / g.w;
                 if (yn < (uint64_t)g.h) {
-                    const int32_t t = fb.rownl[yn];
+                    // last newline writer of row yn: max over the leaf-to-root path
+                    int32_t t = -1;
+                    for (uint32_t i = (uint32_t)yn + (uint32_t)g.nl_size; i >= 1; i >>= 1)
+                        t = max(t, fb.nltree[i]);
                     if (t >= 0) {
                         const Cand n{(uint32_t)t, (int32_t)yn, INT_MAX, (uint32_t)'\n'};
                         if (!have || later(n, best)) best = n;

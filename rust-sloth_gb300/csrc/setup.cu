@@ -5,6 +5,7 @@
 // recomputes utransform*transform per triangle and normal() per covered sample; both
 // are the same value every time, so they are formed once (matrix on the host, normal
 // here) with the same operation order.
+#include "bounds.cuh"
 #include "sloth_internal.cuh"
 #include "sloth_kernels.h"
 
@@ -166,6 +167,7 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, Fra
                             fabsf(p2.y) < big && fabsf(p3.x) < big && fabsf(p3.y) < big;
         r.flags = finite ? kFlagFiniteXY : 0u;
         r.xe = x1;
+        r.zlo = -INFINITY;
         if (finite && r.x0 < x1 && r.y0 < r.y1) {
             // first column strictly right of the triangle, not left of x0
             const float xf = fadd(floorf(mxx), 1.0f);
@@ -176,8 +178,18 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, Fra
                     r.flags |= kFlagTight;
                 }
             }
+            // cull triangles that provably cover no sample of the evaluated range (the
+            // range right of xe is already proven empty, or xe is the reference's bound)
+            if (r.x0 < r.xe) {
+                const OrientBound ob = orient_bound(r);
+                if (provably_empty(ob)) {
+                    r.xe = r.x0;
+                    r.flags |= kFlagCulled;
+                } else {
+                    r.zlo = depth_lower_bound(r, ob);
+                }
+            }
         }
-        r.pad = 0;
         const uint32_t gtri = tri_base + t;
         fb.records[gtri] = r;
 
@@ -195,11 +207,6 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, Fra
                     if (tr >= TU.ya && tr < TU.yb && tc >= TU.xa && tc < TU.xb) continue;
                     if (tile_hit(r, vp, U, W, tr, tc)) atomicAdd(&bb.tile_count[tr * g.ntx + tc], 1u);
                 }
-            // newline sentinels (image mode): max draw index per row, filtered reads first
-            if (g.image)
-                for (int y = r.y0; y < r.y1; ++y)
-                    if (*(volatile int32_t *)&fb.rownl[y] < (int32_t)gtri)
-                        atomicMax(&fb.rownl[y], (int32_t)gtri);
         }
     }
     // warp-ballot compaction of the large-triangle queue
@@ -211,6 +218,69 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, Fra
         base = __shfl_sync(0xffffffffu, base, 0);
         if (large) bb.large_queue[base + __popc(m & ((1u << lane) - 1u))] = t;
     }
+}
+
+// Newline sentinels (src/rasterizer.rs:89-91): in image mode every row y in [y0,y1) of
+// every triangle gets frame cell y*w+1 = '\n' after the row's samples.  The resolve needs,
+// per row, the last triangle in draw order that wrote it: the maximum draw index whose
+// [y0,y1) contains y.  Each triangle folds its interval into a max segment tree with
+// O(log h) node updates (canonical decomposition); a row's value is the maximum over its
+// leaf-to-root path.  Each block builds a tree for a chunk of triangles in shared memory,
+// then merges its non-empty nodes into the frame's tree.
+template <bool kShared>
+__global__ void __launch_bounds__(1024)
+newline_kernel(uint32_t ntri, uint32_t tri_base, uint32_t chunk, FrameGeom g, FrameBuffers fb)
+{
+    extern __shared__ int32_t stree[];
+    const int n = g.nl_size;
+    int32_t *tree = kShared ? stree : fb.nltree;
+    if (kShared) {
+        for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) stree[i] = -1;
+        __syncthreads();
+    }
+    const uint32_t lo = blockIdx.x * chunk, hi = min(ntri, lo + chunk);
+    for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+        const int32_t v = (int32_t)(tri_base + t);
+        const int4 yr = __ldg(reinterpret_cast<const int4 *>(fb.records + tri_base + t) + 4);
+        int l = yr.z + n, r = yr.w + n;   // [y0, y1)
+        while (l < r) {
+            if (l & 1) {
+                if (kShared || *(volatile int32_t *)&tree[l] < v) atomicMax(&tree[l], v);
+                ++l;
+            }
+            if (r & 1) {
+                --r;
+                if (kShared || *(volatile int32_t *)&tree[r] < v) atomicMax(&tree[r], v);
+            }
+            l >>= 1;
+            r >>= 1;
+        }
+    }
+    if (kShared) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) {
+            const int32_t v = stree[i];
+            if (v >= 0 && *(volatile int32_t *)&fb.nltree[i] < v) atomicMax(&fb.nltree[i], v);
+        }
+    }
+}
+
+cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
+                           const FrameBuffers &fb, cudaStream_t s)
+{
+    if (ntri == 0 || !g.image) return cudaSuccess;
+    const uint32_t chunk = 8192;
+    const uint32_t blocks = (ntri + chunk - 1) / chunk;
+    const size_t smem = 2 * (size_t)g.nl_size * sizeof(int32_t);
+    if (smem <= 128 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(newline_kernel<true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024);
+        if (e != cudaSuccess) return e;
+        newline_kernel<true><<<blocks, 1024, smem, s>>>(ntri, tri_base, chunk, g, fb);
+    } else {
+        newline_kernel<false><<<blocks, 1024, 0, s>>>(ntri, tri_base, chunk, g, fb);
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *tv, cudaStream_t s)

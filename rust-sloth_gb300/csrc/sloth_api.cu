@@ -72,6 +72,7 @@ struct sloth_ctx {
     bool dirty = true;
 
     // instrumentation
+    int depth_cull = 1;
     bool timing = false;
     std::map<std::string, KernelClock> clocks;
     uint64_t launches = 0;
@@ -146,7 +147,7 @@ static void free_frame(sloth_ctx *ctx)
 {
     dfree(ctx->fb.keys);
     dfree(ctx->fb.tile_gen);
-    dfree(ctx->fb.rownl);
+    dfree(ctx->fb.nltree);
     dfree(ctx->fb.z_out);
     dfree(ctx->fb.cells_out);
     dfree(ctx->fb.winner_out);
@@ -171,13 +172,15 @@ static sloth_status alloc_frame(sloth_ctx *ctx)
     g.ntx = (g.w + g.tw - 1) / g.tw;
     g.nty = (g.h + g.th - 1) / g.th;
     g.pitch = g.ntx * g.tw;
+    g.nl_size = 1;
+    while (g.nl_size < g.h) g.nl_size <<= 1;
     const size_t ntiles = (size_t)g.ntx * g.nty;
     const size_t nz = (size_t)g.w * g.h;
     const size_t ncells = g.image ? nz + g.h : nz;
     CU(ctx, dalloc(&ctx->fb.keys, (size_t)g.pitch * g.nty * g.th));
     CU(ctx, dalloc(&ctx->fb.tile_gen, ntiles));
     CU(ctx, cudaMemsetAsync(ctx->fb.tile_gen, 0, ntiles * sizeof(uint32_t), ctx->stream));
-    CU(ctx, dalloc(&ctx->fb.rownl, (size_t)g.h));
+    CU(ctx, dalloc(&ctx->fb.nltree, 2 * (size_t)g.nl_size));
     CU(ctx, dalloc(&ctx->fb.z_out, nz));
     CU(ctx, dalloc(&ctx->fb.cells_out, ncells));
     CU(ctx, dalloc(&ctx->fb.winner_out, nz));
@@ -413,7 +416,7 @@ sloth_status sloth_ctx_clear(sloth_ctx *ctx)
         CU(ctx, cudaMemsetAsync(ctx->fb.tile_gen, 0, ctx->ntiles_cap * sizeof(uint32_t), ctx->stream));
         ctx->fb.gen = 1;
     }
-    CU(ctx, cudaMemsetAsync(ctx->fb.rownl, 0xff, (size_t)ctx->g.h * sizeof(int32_t), ctx->stream));
+    CU(ctx, cudaMemsetAsync(ctx->fb.nltree, 0xff, 2 * (size_t)ctx->g.nl_size * sizeof(int32_t), ctx->stream));
     CU(ctx, cudaMemsetAsync(ctx->fb.fragments, 0, sizeof(unsigned long long), ctx->stream));
     ctx->tri_base = 0;
     ctx->dirty = true;
@@ -602,7 +605,8 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     CU(ctx, cudaMemsetAsync(ctx->bb.large_count, 0, sizeof(uint32_t), s));
     CU(ctx, timed(ctx, "vertex", [&] { return launch_vertex_transform(md, M, ctx->tv, s); }));
     CU(ctx, timed(ctx, "setup", [&] { return launch_setup(md, ctx->tv, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
-    CU(ctx, timed(ctx, "bin_count_large", [&] { return launch_bin_count_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+    CU(ctx, timed(ctx, "newline", [&] { return launch_newline(mesh->ntri, ctx->tri_base, g, ctx->fb, s); }));
+    CU(ctx, timed(ctx, "bin_count_large",[&] { return launch_bin_count_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
     CU(ctx, cudaMemcpyAsync(ctx->h_total, ctx->bb.tile_offset + ntiles, sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, s));
@@ -613,7 +617,7 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     ctx->bb.capacity = (uint32_t)(ecap > 0xffffffffu ? 0xffffffffu : ecap);
     CU(ctx, timed(ctx, "bin_fill", [&] { return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_fill_large", [&] { return launch_bin_fill_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
-    CU(ctx, timed(ctx, "raster", [&] { return launch_raster(g, ctx->fb, ctx->bb, s); }));
+    CU(ctx, timed(ctx, "raster", [&] { return launch_raster(g, ctx->fb, ctx->bb, ctx->depth_cull, s); }));
     ctx->tri_base += mesh->ntri;
     ctx->dirty = true;
     return SLOTH_OK;
@@ -622,6 +626,19 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
 // ---------------------------------------------------------------------------------------
 // timing hooks
 // ---------------------------------------------------------------------------------------
+sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    switch (option) {
+    case SLOTH_OPTION_DEPTH_CULL:
+        if (value != 0 && value != 1) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "depth cull is 0 or 1");
+        ctx->depth_cull = (int)value;
+        return SLOTH_OK;
+    default:
+        return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "unknown option %d", option);
+    }
+}
+
 sloth_status sloth_ctx_set_timing(sloth_ctx *ctx, int enable)
 {
     if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;

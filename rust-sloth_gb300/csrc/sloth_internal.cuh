@@ -21,7 +21,6 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 constexpr float kFltMax = 3.40282347e+38f;
 constexpr uint64_t kEmptyKey = ~0ull;
 constexpr uint32_t kSmallMaxTilesDev = 8;   // triangles over more tiles are binned by warps
-constexpr int32_t kSmallMaxRowsDev = 64;    // ... and so are triangles with more newline rows
 
 // orient(a, b, p) of src/rasterizer.rs:30-32 with the edge constants precomputed:
 // (bx-ax)*(py-ay) - (by-ay)*(px-ax) where dx = bx-ax, dy = by-ay.
@@ -62,13 +61,15 @@ struct __align__(16) TriRecord {
     float na;                       // row 5: normal().z * a (shade = na * ((w0+w1)+w2))
     uint32_t rgb;                   // r | g<<8 | b<<16
     uint32_t flags;                 // kFlag*
-    uint32_t pad;
+    float zlo;                      // lower bound of every depth the raster can compute for
+                                    // this triangle, or -inf (bounds.cuh)
 };
 static_assert(sizeof(TriRecord) == 96, "record layout");
 
 constexpr uint32_t kFlagFiniteXY = 1u;   // |x|,|y| of all vertices < 1e18: edge functions are
                                          // monotone and overflow-free, corner tests are exact
 constexpr uint32_t kFlagTight = 2u;      // xe was tightened below the reference's x bound
+constexpr uint32_t kFlagCulled = 4u;     // proven to cover no sample (xe = x0)
 
 // Sample-space edge values for one record at integer sample (px, py).
 struct EdgeVals {
@@ -227,7 +228,7 @@ __device__ __forceinline__ TileSpan tile_span(const Viewport &vp, const TriRecor
             sp.W = Rect{0, 0, 0, 0};
         }
     }
-    sp.large = sp.ntiles > kSmallMaxTilesDev || (vp.image && r.y1 - r.y0 > kSmallMaxRowsDev);
+    sp.large = sp.ntiles > kSmallMaxTilesDev;
     return sp;
 }
 

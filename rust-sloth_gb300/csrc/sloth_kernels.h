@@ -15,13 +15,15 @@ struct TriRecord;
 struct FrameGeom {
     int32_t w, h, image;
     int32_t tw, th, ntx, nty, pitch;
+    int32_t nl_size;         // power of two >= h: leaves of the newline segment tree
 };
 
 // Device buffers of one frame (one Context).
 struct FrameBuffers {
     uint64_t *keys;          // nty*th rows x pitch cells, valid where tile_gen == gen
     uint32_t *tile_gen;      // ntx*nty
-    int32_t *rownl;          // h: max draw index with a newline sentinel in the row, or -1
+    int32_t *nltree;         // 2*nl_size: max segment tree over rows of the draw indices whose
+                             // newline row range [y0,y1) covers each node (-1 = none)
     TriRecord *records;      // draw index -> record
     float *z_out;            // w*h
     uint32_t *cells_out;     // w*h (+h)
@@ -35,7 +37,7 @@ struct BinBuffers {
     uint32_t *tile_count;    // ntiles
     uint32_t *tile_offset;   // ntiles + 1 (exclusive scan; [ntiles] = total entries)
     uint32_t *tile_cursor;   // ntiles
-    uint32_t *entries;       // capacity: draw indices grouped by tile
+    uint64_t *entries;       // capacity: per tile, (ordered depth lower bound << 32 | draw index)
     uint32_t capacity;
     uint32_t *large_queue;   // mesh-local triangle indices of triangles binned by warps
     uint32_t *large_count;   // 1
@@ -61,6 +63,9 @@ cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *
 cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, uint32_t tri_base,
                          const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
                          cudaStream_t s);
+// newline sentinels (image mode): fold each triangle's row range into the segment tree.
+cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
+                           const FrameBuffers &fb, cudaStream_t s);
 cudaError_t launch_bin_count_large(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
                                    const BinBuffers &bb, cudaStream_t s);
 cudaError_t launch_bin_scan(uint32_t ntiles, const BinBuffers &bb, cudaStream_t s);
@@ -70,7 +75,7 @@ cudaError_t launch_bin_fill_large(uint32_t tri_base, const FrameGeom &g, const F
                                   const BinBuffers &bb, cudaStream_t s);
 
 // per-tile raster: 64-bit atomicMin of depth keys in shared memory, merged into keys.
-cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
+cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb, int depth_cull,
                           cudaStream_t s);
 
 // resolve: keys -> z, frame cells, winners.
@@ -79,6 +84,5 @@ cudaError_t launch_resolve(const FrameGeom &g, const FrameBuffers &fb, cudaStrea
 constexpr int kTileW = 64;   // cells (even)
 constexpr int kTileH = 32;   // rows
 constexpr uint32_t kSmallMaxTiles = 8;   // triangles over more tiles are binned by warps
-constexpr int32_t kSmallMaxRows = 64;    // ... and so are triangles with more newline rows
 
 }  // namespace sloth

@@ -20,7 +20,8 @@ HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libsloth_gpu.so"
 
 OK = 0
-STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "LIMIT", 5: "DEVICE_FAULT"}
+OPTION_DEPTH_CULL = 1
+STATUS ={0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "LIMIT", 5: "DEVICE_FAULT"}
 
 # Every symbol declared in include/sloth_gpu.h, with (restype, argtypes).
 _f32p = C.POINTER(C.c_float)
@@ -54,6 +55,7 @@ SIGNATURES = {
     "sloth_mesh_info": (C.c_int, [_vp, _u32p, _f32p]),
     "sloth_mesh_update": (C.c_int, [_vp, _f32p, _f32p, _f32p, _u8p]),
     "sloth_draw_mesh": (C.c_int, [_vp, _vp, _f32p]),
+    "sloth_ctx_set_option": (C.c_int, [_vp, C.c_int, C.c_int64]),
     "sloth_ctx_set_timing": (C.c_int, [_vp, C.c_int]),
     "sloth_ctx_kernel_time": (C.c_int, [_vp, C.c_char_p, C.POINTER(C.c_double), _u64p]),
     "sloth_ctx_launch_count": (C.c_uint64, [_vp]),
@@ -206,6 +208,10 @@ class Context:
         f = C.c_uint64()
         self._check(self.lib.sloth_ctx_fragments(self.h, C.byref(f)))
         return f.value
+
+    def set_depth_cull(self, on: bool):
+        """SLOTH_OPTION_DEPTH_CULL: skip triangles proven hidden (same results)."""
+        self._check(self.lib.sloth_ctx_set_option(self.h, OPTION_DEPTH_CULL, 1 if on else 0))
 
     def set_timing(self, on: bool):
         self._check(self.lib.sloth_ctx_set_timing(self.h, 1 if on else 0))

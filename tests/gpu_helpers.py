@@ -6,22 +6,42 @@ import sloth_gpu as S
 from oracle import oracle as O
 
 
-def gpu_render(ctx, meshes, R, w, h, image, U=None, dev_meshes=None):
-    """Clear, draw every mesh in order, read back.  Returns (cells, z, winner, fragments)."""
+def _render_once(ctx, dev_meshes, Rs, w, h, image, U, depth_cull):
+    ctx.set_depth_cull(depth_cull)
     ctx.set_viewport(w, h, image)
-    if dev_meshes is None:
-        dev_meshes = [S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"], m.get("idx"), m.get("bbox_max"))
-                      for m in meshes]
     if U is None:
         ctx.update(dev_meshes)
     else:
         ctx.set_utransform(U)
     ctx.clear()
-    Rs = R if isinstance(R, list) else [R] * len(dev_meshes)
     for dm, Rm in zip(dev_meshes, Rs):
         ctx.draw_mesh(dm, Rm)
     cells, z, winner = ctx.read()
     return cells, z, winner, ctx.fragments()
+
+
+def gpu_render(ctx, meshes, R, w, h, image, U=None, dev_meshes=None, depth_cull=None):
+    """Clear, draw every mesh in order, read back: (cells, z, winner, fragments).
+
+    depth_cull None renders twice, without depth culling (where every covered sample is
+    counted, so the fragment count is compared) and with it (buffers must be identical);
+    the returned tuple is the culled render with the unculled fragment count."""
+    if dev_meshes is None:
+        dev_meshes = [S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"], m.get("idx"), m.get("bbox_max"))
+                      for m in meshes]
+    Rs = R if isinstance(R, list) else [R] * len(dev_meshes)
+    if depth_cull is not None:
+        out = _render_once(ctx, dev_meshes, Rs, w, h, image, U, depth_cull)
+        return out if not depth_cull else (*out[:3], None)
+    plain = _render_once(ctx, dev_meshes, Rs, w, h, image, U, False)
+    culled = _render_once(ctx, dev_meshes, Rs, w, h, image, U, True)
+    for a, b, name in zip(plain[:3], culled[:3], ("cells", "z", "winner")):
+        assert np.array_equal(a.view(np.uint32) if a.dtype == np.float32 else a,
+                              b.view(np.uint32) if b.dtype == np.float32 else b), \
+            f"depth culling changed the {name} buffer"
+    assert culled[3] <= plain[3]
+    ctx.set_depth_cull(True)
+    return (*culled[:3], plain[3])
 
 
 def oracle_render(meshes, R, w, h, image, U=None, threads=1):
@@ -44,4 +64,5 @@ def assert_same(gpu, ref, label=""):
            f"first z {bad_z[:5].tolist()} gpu {z[bad_z[:5]].tolist()} ref {ref.z[bad_z[:5]].tolist()}; "
            f"winners gpu {winner[bad_w[:5]].tolist()} ref {ref.winner[bad_w[:5]].tolist()}")
     assert bad_c.size == 0 and bad_z.size == 0 and bad_w.size == 0, msg
-    assert frags == ref.fragments, f"{label}: fragments gpu {frags} ref {ref.fragments}"
+    if frags is not None:
+        assert frags == ref.fragments, f"{label}: fragments gpu {frags} ref {ref.fragments}"

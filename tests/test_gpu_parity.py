@@ -124,6 +124,10 @@ def test_scaled_config2_soup(ctx, w, h):
     for image in (True, False):
         ref = oracle_render([m], R, w, h, image)
         assert_same(gpu_render(ctx, [m], R, w, h, image), ref, f"soup {w}x{h}")
+    # the depth culling is active here: it skips some of the covered samples
+    culled = gpu_render(ctx, [m], R, w, h, True, depth_cull=True)
+    ctx.set_depth_cull(True)
+    assert ctx.fragments() < ref.fragments
 
 
 def test_yawed_soup_wraps(ctx):
@@ -165,6 +169,7 @@ def test_many_frames_generation_counter(ctx):
     """Repeated clears reuse the key buffer through the tile generation counter."""
     m = W.soup(300, seed=1)
     ctx.set_viewport(64, 32, True)
+    ctx.set_depth_cull(False)   # every covered sample counted
     dm = S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"])
     ctx.update([dm])
     ang = np.linspace(0, 2 * math.pi, 12)
@@ -175,6 +180,7 @@ def test_many_frames_generation_counter(ctx):
         cells, z, winner = ctx.read()
         ref = oracle_render([m], R, 64, 32, True)
         assert_same((cells, z, winner, ctx.fragments()), ref, f"angle {a}")
+    ctx.set_depth_cull(True)
     # an empty frame after drawing: clear only
     ctx.clear()
     cells, z, winner = ctx.read()
