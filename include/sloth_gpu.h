@@ -160,6 +160,40 @@ sloth_status sloth_mesh_info(const sloth_mesh *mesh, uint32_t *ntri, float bbox_
  * utransform*transform once, in nalgebra's order.  Asynchronous on the ctx stream. */
 sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float transform[16]);
 
+/* ---- one frame without device allocation ------------------------------------------ */
+
+/* No counterpart in the reference.  For callers that cannot let a library allocate
+ * device memory: hosts that fix the renderer's memory at start-up and forbid allocation
+ * afterwards, frame loops that cannot afford the device-wide synchronisation of
+ * cudaMalloc/cudaFree, and programs whose memory is held by a framework's caching pool.
+ *
+ * Draws one unindexed triangle soup (triangle t = vertices 3t..3t+2 of x, y, z; face
+ * colours rgb, 3 per triangle) into a cleared width x height context and writes its
+ * frame cells (cells: w*h, or w*h+h in image mode), depth buffer (zbuf: w*h) and winners
+ * (winner: w*h) -- the same values as sloth_ctx_clear + sloth_draw_mesh + sloth_ctx_read.
+ * m = utransform*transform, row-major, in host memory.  Every other pointer is device
+ * memory owned by the caller.  Work is queued on `stream` (a cudaStream_t, NULL = the
+ * default stream); the call returns without waiting for it.
+ *
+ * It calls no cudaMalloc or cudaFree: all intermediate buffers live in one __device__
+ * array of SLOTH_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library holds
+ * until the process exits.  Limits: ntri <= SLOTH_NOALLOC_MAX_TRIANGLES,
+ * height <= SLOTH_NOALLOC_MAX_HEIGHT, and the viewport padded to 64x32-cell tiles
+ * ((ceil(w/64)*64) * (ceil(h/32)*32)) <= SLOTH_NOALLOC_MAX_DEPTH_CELLS; larger inputs
+ * return SLOTH_ERR_LIMIT.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture.  All calls share the array, so calls that overlap on the GPU (on
+ * different streams, or from different threads) race and corrupt each other's frames:
+ * issue them one after another. */
+#define SLOTH_NOALLOC_MAX_TRIANGLES 32768u
+#define SLOTH_NOALLOC_MAX_HEIGHT 4096u
+#define SLOTH_NOALLOC_MAX_DEPTH_CELLS 524288u
+#define SLOTH_NOALLOC_SCRATCH_BYTES 9081600u
+sloth_status sloth_render_noalloc(const float *x, const float *y, const float *z, uint32_t ntri,
+                                  const uint8_t *rgb, const float m[16], uint32_t width,
+                                  uint32_t height, int image, uint32_t *cells, float *zbuf,
+                                  int32_t *winner, void *stream);
+
 /* ---- timing hooks for benchmarks -------------------------------------------------- */
 
 /* Enable (1) / disable (0) CUDA-event timing of each kernel the context launches.

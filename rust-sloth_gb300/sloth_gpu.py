@@ -56,6 +56,8 @@ SIGNATURES = {
     "sloth_mesh_update": (C.c_int, [_vp, _f32p, _f32p, _f32p, _u8p]),
     "sloth_draw_mesh": (C.c_int, [_vp, _vp, _f32p]),
     "sloth_ctx_set_option": (C.c_int, [_vp, C.c_int, C.c_int64]),
+    "sloth_render_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_uint32, _vp, _f32p, C.c_uint32, C.c_uint32,
+                                       C.c_int, _vp, _vp, _vp, _vp]),
     "sloth_ctx_set_timing": (C.c_int, [_vp, C.c_int]),
     "sloth_ctx_kernel_time": (C.c_int, [_vp, C.c_char_p, C.POINTER(C.c_double), _u64p]),
     "sloth_ctx_launch_count": (C.c_uint64, [_vp]),
