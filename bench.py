@@ -54,6 +54,20 @@ def dist_env():
     return ws, rank, local
 
 
+WORKLOADS = {
+    # name: (description, width, height, small triangles, large triangles)
+    "config2": (WORKLOAD, 3840, 2160, 1_000_000, 2_000),
+    # a quarter of config 2 (same statistics) for kernel profiling under ncu
+    "config2-quarter": ("config2 statistics at a quarter: 250k + 500 large triangles, 1920x1080 image mode",
+                        1920, 1080, 250_000, 500),
+}
+
+
+def select_workload(name: str):
+    global WORKLOAD, W_PX, H_PX, N_SMALL, N_LARGE
+    WORKLOAD, W_PX, H_PX, N_SMALL, N_LARGE = WORKLOADS[name]
+
+
 def make_workload():
     import workloads as W
     m = W.soup(N_SMALL, seed=SEED, n_large=N_LARGE)
@@ -83,7 +97,7 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                 "-lms", "20"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
@@ -284,22 +298,23 @@ def run_gpu(args):
         ctx.draw_mesh(dm, R)
         ctx.read_into(hcells, hzbuf)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    if ws > 1:
-        torch.distributed.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_fps = ws * args.steps / e2e_s
+    e2e = None
+    if not args.no_e2e:
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        if ws > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = time.perf_counter() - t0
+        if ws > 1:
+            t = torch.tensor([e2e_s], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": ws * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
 
-    # parity spot check of the benchmarked frame against a banded oracle sample is in
-    # the gpu tests; here we only confirm the output is non-trivial
     if rank != 0:
         if ws > 1:
             torch.distributed.destroy_process_group()
@@ -332,7 +347,7 @@ def run_gpu(args):
         "gfrag_per_s": frags * value / 1e9, "fragments_per_frame": frags,
         "fragments_rasterized_per_frame": frags_evaluated,
         "depth_cull": not args.no_depth_cull,
-        "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": e2e,
         "gpu_launches": launches, "kernels": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
     }
     print(json.dumps(line), flush=True)
@@ -345,7 +360,7 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-den", type=int, default=8)
@@ -353,7 +368,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-depth-cull", action="store_true",
                     help="rasterize every triangle (SLOTH_OPTION_DEPTH_CULL 0)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
+    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    select_workload(args.workload)
     if args.impl == "reference":
         return run_reference(args)
     import __graft_entry__ as g

@@ -130,7 +130,14 @@ sloth_status sloth_ctx_fragments(sloth_ctx *ctx, uint64_t *fragments);
  *   behind every depth cell they could write (a proven depth bound against the tile's
  *   current depths); 0 rasterizes every triangle.  Results are identical either way. */
 #define SLOTH_OPTION_DEPTH_CULL 1
+/* SLOTH_OPTION_TILE_SHAPE: index of the raster's tile shape (see sloth_tile_shape; 0 is
+ *   64 cells x 32 rows); takes effect at the next sloth_ctx_clear. */
+#define SLOTH_OPTION_TILE_SHAPE 2
 sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value);
+
+/* The raster tile shapes the library is built for: shape i is `cells` depth cells wide
+ * and `rows` rows high; SLOTH_ERR_INVALID_ARGUMENT past the last shape. */
+sloth_status sloth_tile_shape(int shape, uint32_t *cells, uint32_t *rows);
 
 /* ---- meshes (SimpleMesh, src/geometry.rs:78-81) ------------------------------------ */
 
@@ -159,6 +166,54 @@ sloth_status sloth_mesh_info(const sloth_mesh *mesh, uint32_t *ntri, float bbox_
  * transform: the row-major rotation (or any model matrix); the library forms
  * utransform*transform once, in nalgebra's order.  Asynchronous on the ctx stream. */
 sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float transform[16]);
+
+/* ---- many frames at once --------------------------------------------------------- */
+
+/* The reference renders frame after frame (src/main.rs:60-111: update, clear, draw every
+ * mesh of the queue, flush); its multi-frame JS export (`image -j N`, src/main.rs:55-58,
+ * 92-106) and multi-model queues (src/inputs.rs:95-129) repeat that loop.  A batch holds
+ * many such frames -- views, meshes and viewports of uneven sizes -- and renders all of
+ * them with one pass of each stage and one persistent raster pass over a device-side
+ * (frame, tile) queue, replayed as a CUDA graph.  Every frame is bit-identical to
+ * clear + draw_mesh of its draws in order on a context with the same viewport. */
+typedef struct sloth_batch sloth_batch;
+
+typedef struct sloth_draw_desc {
+    const sloth_mesh *mesh;    /* draw_mesh(context, mesh, transform, default_shader) */
+    float transform[16];       /* row-major */
+} sloth_draw_desc;
+
+typedef struct sloth_frame_desc {
+    uint32_t width, height;    /* Context.width/height */
+    int32_t image;             /* Context.image */
+    float utransform[16];      /* Context.utransform, row-major */
+    uint32_t first_draw;       /* the frame draws draws[first_draw .. first_draw+ndraws) in order; */
+    uint32_t ndraws;           /* frames list consecutive ranges starting at draw 0 */
+} sloth_frame_desc;
+
+/* Lay out a batch on the context's device and stream (the meshes must outlive it). */
+sloth_status sloth_batch_create(sloth_ctx *ctx, const sloth_frame_desc *frames, uint32_t nframes,
+                                const sloth_draw_desc *draws, uint32_t ndraws, sloth_batch **out);
+void sloth_batch_destroy(sloth_batch *batch);
+/* Replace every draw's transform (16 floats per draw); waits for the previous render. */
+sloth_status sloth_batch_set_transforms(sloth_batch *batch, const float *transforms);
+/* Render every frame (asynchronous on the context's stream).  The first render sizes the
+ * tile-entry buffer (one host synchronisation); later renders replay a CUDA graph. */
+sloth_status sloth_batch_render(sloth_batch *batch);
+/* Copy one frame's buffers to host memory (any may be NULL); blocks.  If the last render
+ * outgrew the tile-entry buffer, it is re-planned and re-rendered first. */
+sloth_status sloth_batch_read(sloth_batch *batch, uint32_t frame, uint32_t *cells, float *z, int32_t *winner);
+/* Device pointers of one frame's resolved buffers. */
+sloth_status sloth_batch_frame_buffers(sloth_batch *batch, uint32_t frame, const uint32_t **cells,
+                                       const float **z);
+/* Fragments the raster evaluated in the last render, summed over frames (see
+ * sloth_ctx_fragments); blocks. */
+sloth_status sloth_batch_fragments(sloth_batch *batch, uint64_t *fragments);
+/* Use tile shape `shape` (sloth_tile_shape) for this batch; re-lays out its buffers. */
+sloth_status sloth_batch_set_tile_shape(sloth_batch *batch, int shape);
+/* Autotuner: render the batch `reps` times with every tile shape, keep the fastest;
+ * reports the shape and its mean render time in ms. */
+sloth_status sloth_batch_autotune(sloth_batch *batch, int reps, int *best_shape, float *best_ms);
 
 /* ---- one frame without device allocation ------------------------------------------ */
 

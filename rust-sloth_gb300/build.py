@@ -18,7 +18,8 @@ INCLUDE = HERE.parent / "include"
 OUT_DIR = HERE / "_build"
 LIB = OUT_DIR / "libsloth_gpu.so"
 
-SOURCES = ["setup.cu", "bin.cu", "raster.cu", "resolve.cu", "sloth_api.cu", "noalloc.cu"]
+SOURCES = ["setup.cu", "bin.cu", "raster.cu", "resolve.cu", "sloth_api.cu", "noalloc.cu", "batch.cu",
+           "batch_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-ftz=false",

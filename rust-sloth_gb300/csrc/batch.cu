@@ -1,0 +1,267 @@
+// batch.cu -- kernels of the batched path: many frames (views, meshes, viewports) in one
+// pass of each stage, and one persistent raster kernel over a device-side (frame, tile)
+// work queue.  Every per-triangle, per-tile and per-cell step is the single-frame one
+// (record.cuh, bin_common.cuh, raster_common.cuh, resolve_common.cuh) applied to the
+// item's frame, so each frame is bit-identical to drawing it alone.
+#include "batch_kernels.h"
+#include "bin_common.cuh"
+#include "raster_common.cuh"
+#include "record.cuh"
+#include "resolve_common.cuh"
+
+namespace sloth {
+
+__device__ __forceinline__ Viewport vp_batch(const FrameGeom &g)
+{
+    return Viewport{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
+}
+
+// blocks[i] = (draw, first vertex quad): four vertices per thread, float4 SoA loads.
+__global__ void __launch_bounds__(256) batch_vertex_kernel(BatchDev b, const int2 *__restrict__ blocks)
+{
+    const int2 blk = blocks[blockIdx.x];
+    const BatchDraw &d = b.draws[blk.x];
+    const Mat4 M = b.mats[blk.x];
+    const uint32_t nv = d.mesh.nvert;
+    const uint32_t q = (uint32_t)blk.y + threadIdx.x;
+    const uint32_t i0 = q * 4;
+    if (i0 >= nv) return;
+    float xs[4], ys[4], zs[4];
+    if (i0 + 4 <= nv) {
+        const float4 X = __ldg(reinterpret_cast<const float4 *>(d.mesh.x) + q);
+        const float4 Y = __ldg(reinterpret_cast<const float4 *>(d.mesh.y) + q);
+        const float4 Z = __ldg(reinterpret_cast<const float4 *>(d.mesh.z) + q);
+        xs[0] = X.x; xs[1] = X.y; xs[2] = X.z; xs[3] = X.w;
+        ys[0] = Y.x; ys[1] = Y.y; ys[2] = Y.z; ys[3] = Y.w;
+        zs[0] = Z.x; zs[1] = Z.y; zs[2] = Z.z; zs[3] = Z.w;
+    } else {
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = i0 + k < nv ? i0 + k : nv - 1;
+            xs[k] = d.mesh.x[i]; ys[k] = d.mesh.y[i]; zs[k] = d.mesh.z[i];
+        }
+    }
+    float4 *tv = b.tv + d.vert_off;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (i0 + k < nv)
+            tv[i0 + k] = make_float4(row_dot(&M.m[0], xs[k], ys[k], zs[k]), row_dot(&M.m[4], xs[k], ys[k], zs[k]),
+                                     row_dot(&M.m[8], xs[k], ys[k], zs[k]), 0.0f);
+}
+
+// blocks[i] = (draw, first triangle): records, small-triangle tile counts, large queue.
+__global__ void __launch_bounds__(kBatchSetupBlock) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
+{
+    const int2 blk = blocks[blockIdx.x];
+    const BatchDraw &d = b.draws[blk.x];
+    const BatchFrame &f = b.frames[d.frame];
+    const uint32_t t = (uint32_t)blk.y + threadIdx.x;
+    bool large = false;
+    if (t < d.mesh.ntri) {
+        uint32_t i1, i2, i3;
+        if (d.mesh.idx) {
+            i1 = __ldg(d.mesh.idx + 3 * (size_t)t + 0);
+            i2 = __ldg(d.mesh.idx + 3 * (size_t)t + 1);
+            i3 = __ldg(d.mesh.idx + 3 * (size_t)t + 2);
+        } else {
+            i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
+        }
+        const float4 *tv = b.tv + d.vert_off;
+        const TriRecord r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3),
+                                         d.mesh.rgb + 3 * (size_t)t, f.g.w, f.g.h);
+        f.fb.records[d.local_base + t] = r;
+        const Viewport vp = vp_batch(f.g);
+        const TileSpan sp = tile_span(vp, r);
+        large = sp.large;
+        if (!large) count_small_tiles(r, vp, sp, b.bb.tile_count + f.tile_off);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, large);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(b.bb.large_count, (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (large) {
+            const uint32_t q = base + __popc(m & ((1u << lane) - 1u));
+            b.bb.large_queue[q] = d.local_base + t;   // frame-local draw index
+            b.large_frame[q] = d.frame;
+        }
+    }
+}
+
+// blocks[i] = (draw, first triangle of a chunk): newline segment tree of the draw's frame.
+template <bool kShared>
+__global__ void __launch_bounds__(1024) batch_newline_kernel(BatchDev b, const int2 *__restrict__ blocks)
+{
+    extern __shared__ int32_t stree[];
+    const int2 blk = blocks[blockIdx.x];
+    const BatchDraw &d = b.draws[blk.x];
+    const BatchFrame &f = b.frames[d.frame];
+    if (!f.g.image) return;
+    const int n = f.g.nl_size;
+    int32_t *tree = kShared ? stree : f.fb.nltree;
+    if (kShared) {
+        for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) stree[i] = -1;
+        __syncthreads();
+    }
+    const uint32_t lo = (uint32_t)blk.y, hi = min(d.mesh.ntri, lo + kBatchNewlineChunk);
+    for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+        const int32_t v = (int32_t)(d.local_base + t);
+        const int4 yr = __ldg(reinterpret_cast<const int4 *>(f.fb.records + d.local_base + t) + 4);
+        nltree_update(tree, n, yr.z, yr.w, v, kShared);
+    }
+    if (kShared) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) {
+            const int32_t v = stree[i];
+            if (v >= 0 && *(volatile int32_t *)&f.fb.nltree[i] < v) atomicMax(&f.fb.nltree[i], v);
+        }
+    }
+}
+
+// One warp per queued large triangle, any frame.
+template <bool kFill>
+__global__ void __launch_bounds__(256) batch_bin_large_kernel(BatchDev b)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nq = *b.bb.large_count;
+    for (uint32_t q = warp; q < nq; q += nwarps) {
+        const BatchFrame &f = b.frames[b.large_frame[q]];
+        const uint32_t gtri = b.bb.large_queue[q];
+        bin_large_warp<kFill>(f.fb.records[gtri], gtri, vp_batch(f.g), b.bb.tile_count + f.tile_off,
+                              b.bb.tile_cursor + f.tile_off, b.bb.entries, b.bb.capacity, lane);
+    }
+}
+
+// blocks[i] = (draw, first triangle): small triangles' tile entries.
+__global__ void __launch_bounds__(kBatchSetupBlock) batch_fill_kernel(BatchDev b, const int2 *__restrict__ blocks)
+{
+    const int2 blk = blocks[blockIdx.x];
+    const BatchDraw &d = b.draws[blk.x];
+    const uint32_t t = (uint32_t)blk.y + threadIdx.x;
+    if (t >= d.mesh.ntri) return;
+    const BatchFrame &f = b.frames[d.frame];
+    const uint32_t gtri = d.local_base + t;
+    const TriRecord r = f.fb.records[gtri];
+    const Viewport vp = vp_batch(f.g);
+    const TileSpan sp = tile_span(vp, r);
+    if (sp.large || sp.ntiles == 0) return;
+    fill_small(r, gtri, vp, sp, b.bb.tile_cursor + f.tile_off, b.bb.entries, b.bb.capacity);
+}
+
+// Persistent raster: CTAs take (frame, tile) items from a device-side queue until it is
+// empty.  Empty tiles cost one counter read.
+template <int TW, int TH>
+__global__ void __launch_bounds__(kRasterThreads) batch_raster_kernel(BatchDev b)
+{
+    __shared__ TileSmem<TW, TH> S;
+    __shared__ uint32_t s_item;
+    if (b.bb.tile_offset[b.total_tiles] > b.bb.capacity) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *b.overflow = 1;
+        return;
+    }
+    for (;;) {
+        if (threadIdx.x == 0) {
+            uint32_t it;
+            do {
+                it = atomicAdd(b.queue_head, 1u);
+            } while (it < b.total_tiles && b.bb.tile_count[it] == 0);
+            s_item = it;
+        }
+        __syncthreads();
+        const uint32_t item = s_item;
+        __syncthreads();
+        if (item >= b.total_tiles) break;
+        // frame of the global tile: last frame whose first tile is <= item
+        uint32_t lo = 0, hi = b.nframes;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (b.frame_tile_off[mid] <= item) lo = mid;
+            else hi = mid;
+        }
+        const BatchFrame &f = b.frames[lo];
+        raster_tile<TW, TH>(S, f.g, f.fb, (int)(item - f.tile_off), b.bb.tile_count[item],
+                            b.bb.entries + b.bb.tile_offset[item], b.depth_cull);
+    }
+}
+
+// blocks[i] = (frame, first cell).
+__global__ void __launch_bounds__(256) batch_resolve_kernel(BatchDev b, const int2 *__restrict__ blocks)
+{
+    const int2 blk = blocks[blockIdx.x];
+    const BatchFrame &f = b.frames[blk.x];
+    const uint64_t nz = (uint64_t)f.g.w * f.g.h;
+    const uint64_t ncells = f.g.image ? nz + f.g.h : nz;
+    const uint64_t end = min(ncells, (uint64_t)blk.y + kBatchResolveChunk);
+    for (uint64_t c = (uint64_t)blk.y + threadIdx.x; c < end; c += blockDim.x) resolve_cell(f.g, f.fb, c);
+}
+
+cudaError_t prepare_batch_kernels()
+{
+    return cudaFuncSetAttribute(batch_newline_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                128 * 1024);
+}
+
+cudaError_t launch_batch_vertex(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s)
+{
+    if (!nblocks) return cudaSuccess;
+    batch_vertex_kernel<<<nblocks, 256, 0, s>>>(b, blocks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_setup(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s)
+{
+    if (!nblocks) return cudaSuccess;
+    batch_setup_kernel<<<nblocks, kBatchSetupBlock, 0, s>>>(b, blocks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_newline(const BatchDev &b, const int2 *blocks, uint32_t nblocks, int max_nl,
+                                 cudaStream_t s)
+{
+    if (!nblocks) return cudaSuccess;
+    const size_t smem = 2 * (size_t)max_nl * sizeof(int32_t);
+    if (smem <= 128 * 1024) batch_newline_kernel<true><<<nblocks, 1024, smem, s>>>(b, blocks);
+    else batch_newline_kernel<false><<<nblocks, 1024, 0, s>>>(b, blocks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s)
+{
+    if (fill) batch_bin_large_kernel<true><<<2 * 152, 256, 0, s>>>(b);
+    else batch_bin_large_kernel<false><<<2 * 152, 256, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s)
+{
+    if (!nblocks) return cudaSuccess;
+    batch_fill_kernel<<<nblocks, kBatchSetupBlock, 0, s>>>(b, blocks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, cudaStream_t s)
+{
+    if (!b.total_tiles) return cudaSuccess;
+    // persistent: as many CTAs as fit on the GPU (152 SMs x 4 resident CTAs), never more
+    // than there are tiles
+    const uint32_t grid = b.total_tiles < 152u * 4u ? b.total_tiles : 152u * 4u;
+#define SLOTH_BATCH_RASTER_CASE(W_, H_)                                                        \
+    if (tw == W_ && th == H_) {                                                                \
+        batch_raster_kernel<W_, H_><<<grid, kRasterThreads, 0, s>>>(b);                        \
+        return cudaGetLastError();                                                             \
+    }
+    SLOTH_TILE_SHAPES(SLOTH_BATCH_RASTER_CASE)
+#undef SLOTH_BATCH_RASTER_CASE
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_batch_resolve(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s)
+{
+    if (!nblocks) return cudaSuccess;
+    batch_resolve_kernel<<<nblocks, 256, 0, s>>>(b, blocks);
+    return cudaGetLastError();
+}
+
+}  // namespace sloth

@@ -1,0 +1,567 @@
+// batch_api.cu -- sloth_batch_*: many frames, views and meshes per launch sequence.
+//
+// The reference renders one frame at a time (src/main.rs:60-111: update, clear, draw
+// every mesh of the queue, flush); its multi-frame export (`image -j N`) and multi-model
+// queues repeat that loop.  A batch holds many such frames at once -- each with its own
+// viewport, image mode, utransform and ordered draws -- and renders all of them with one
+// pass of each kernel and one persistent raster pass over a device-side (frame, tile)
+// queue.  After the first render (which sizes the tile-entry buffer on the host) the
+// whole sequence is captured in a CUDA graph and replayed.  If a later render's entries
+// outgrow the buffer, the raster reports it and the next read re-plans and re-renders.
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "batch_kernels.h"
+#include "sloth_gpu.h"
+#include "sloth_internal.cuh"
+
+using namespace sloth;
+
+struct sloth_batch {
+    sloth_ctx *ctx = nullptr;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<sloth_frame_desc> frames;
+    std::vector<const sloth_mesh *> meshes;   // per draw
+    std::vector<float> transforms;            // 16 per draw
+    int shape = 0;
+
+    // layout (per shape)
+    std::vector<BatchFrame> hframes;
+    std::vector<uint64_t> cell_off, z_off;    // per frame
+    uint32_t total_tiles = 0;
+    uint64_t total_cells = 0, total_z = 0, total_keys = 0, total_nl = 0, total_rec = 0, total_vert = 0;
+    int max_nl = 1;
+
+    // device memory
+    BatchFrame *d_frames = nullptr;
+    BatchDraw *d_draws = nullptr;
+    Mat4 *d_mats = nullptr;
+    Mat4 *h_mats = nullptr;                   // pinned
+    float4 *tv = nullptr;
+    TriRecord *records = nullptr;
+    uint64_t *keys = nullptr;
+    uint32_t *tile_gen = nullptr;
+    int32_t *nltree = nullptr;
+    float *z = nullptr;
+    uint32_t *cells = nullptr;
+    int32_t *winner = nullptr;
+    unsigned long long *fragments = nullptr;
+    uint32_t *frame_tile_off = nullptr;
+    BinBuffers bb{};
+    size_t entries_cap = 0;
+    uint32_t *large_frame = nullptr;
+    uint32_t *queue_head = nullptr;
+    uint32_t *overflow = nullptr;
+    uint32_t *h_total = nullptr;              // pinned
+    uint32_t *h_overflow = nullptr;           // pinned
+    int2 *blk[4] = {nullptr, nullptr, nullptr, nullptr};   // vertex, triangle, newline, resolve
+    uint32_t nblk[4] = {0, 0, 0, 0};
+
+    cudaGraphExec_t graph = nullptr;
+    bool rendered = false;
+};
+
+// Shared with sloth_api.cu.
+extern "C++" {
+sloth_status sloth_ctx_fail(sloth_ctx *ctx, sloth_status st, const char *msg);
+int sloth_ctx_device(const sloth_ctx *ctx);
+cudaStream_t sloth_ctx_stream(const sloth_ctx *ctx);
+int sloth_ctx_depth_cull(const sloth_ctx *ctx);
+struct MeshView {
+    const float *x, *y, *z;
+    const uint32_t *idx;
+    const uint8_t *rgb;
+    uint32_t nvert, ntri;
+    int device;
+};
+MeshView sloth_mesh_view(const sloth_mesh *m);
+}
+
+namespace {
+
+#define BCU(b, call)                                                                           \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return sloth_ctx_fail((b)->ctx, e_ == cudaErrorMemoryAllocation ? SLOTH_ERR_OUT_OF_MEMORY \
+                                                                            : SLOTH_ERR_CUDA,  \
+                                  (std::string(#call) + ": " + cudaGetErrorString(e_)).c_str()); \
+    } while (0)
+
+template <class T>
+cudaError_t balloc(T **p, size_t n)
+{
+    *p = nullptr;
+    return cudaMalloc(reinterpret_cast<void **>(p), (n ? n : 1) * sizeof(T));
+}
+template <class T>
+void bfree(T *&p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+void free_layout(sloth_batch *b)
+{
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    bfree(b->d_frames);
+    bfree(b->d_draws);
+    bfree(b->d_mats);
+    bfree(b->tv);
+    bfree(b->records);
+    bfree(b->keys);
+    bfree(b->tile_gen);
+    bfree(b->nltree);
+    bfree(b->z);
+    bfree(b->cells);
+    bfree(b->winner);
+    bfree(b->fragments);
+    bfree(b->frame_tile_off);
+    bfree(b->bb.tile_count);
+    bfree(b->bb.tile_offset);
+    bfree(b->bb.tile_cursor);
+    bfree(b->bb.entries);
+    bfree(b->bb.large_queue);
+    bfree(b->bb.large_count);
+    bfree(b->large_frame);
+    bfree(b->queue_head);
+    bfree(b->overflow);
+    for (auto &p : b->blk) bfree(p);
+    b->entries_cap = 0;
+    b->rendered = false;
+}
+
+void set_mats(sloth_batch *b)
+{
+    for (size_t f = 0; f < b->frames.size(); ++f) {
+        const sloth_frame_desc &fd = b->frames[f];
+        for (uint32_t k = 0; k < fd.ndraws; ++k) {
+            const uint32_t d = fd.first_draw + k;
+            sloth_mat4_mul(fd.utransform, &b->transforms[16 * (size_t)d], b->h_mats[d].m);
+        }
+    }
+}
+
+// Lay out every frame for tile shape `shape` and allocate the batch's buffers.
+sloth_status build(sloth_batch *b, int shape)
+{
+    free_layout(b);
+    b->shape = shape;
+    const int tw = kTileShapes[shape][0], th = kTileShapes[shape][1];
+    const uint32_t nf = (uint32_t)b->frames.size(), nd = (uint32_t)b->meshes.size();
+    b->hframes.assign(nf, BatchFrame{});
+    b->cell_off.assign(nf + 1, 0);
+    b->z_off.assign(nf + 1, 0);
+    std::vector<uint64_t> key_off(nf), nl_off(nf), rec_off(nf);
+    std::vector<uint32_t> tile_off(nf + 1, 0);
+    std::vector<BatchDraw> hd(nd);
+    uint64_t keys = 0, nl = 0, rec = 0, vert = 0, cells = 0, zs = 0;
+    uint32_t tiles = 0;
+    b->max_nl = 1;
+    std::vector<int2> bv, bt, bn, br;
+    for (uint32_t f = 0; f < nf; ++f) {
+        const sloth_frame_desc &fd = b->frames[f];
+        FrameGeom g{};
+        g.w = (int32_t)fd.width;
+        g.h = (int32_t)fd.height;
+        g.image = fd.image ? 1 : 0;
+        g.tw = tw;
+        g.th = th;
+        g.ntx = (g.w + tw - 1) / tw;
+        g.nty = (g.h + th - 1) / th;
+        g.pitch = g.ntx * tw;
+        g.nl_size = 1;
+        while (g.nl_size < g.h) g.nl_size <<= 1;
+        b->max_nl = g.nl_size > b->max_nl ? g.nl_size : b->max_nl;
+        BatchFrame &bf = b->hframes[f];
+        bf.g = g;
+        bf.tile_off = tiles;
+        bf.rec_off = (uint32_t)rec;
+        tile_off[f] = tiles;
+        key_off[f] = keys;
+        nl_off[f] = nl;
+        rec_off[f] = rec;
+        b->cell_off[f] = cells;
+        b->z_off[f] = zs;
+        tiles += (uint32_t)(g.ntx * g.nty);
+        keys += (uint64_t)g.pitch * g.nty * th;
+        nl += 2 * (uint64_t)g.nl_size;
+        const uint64_t nz = (uint64_t)g.w * g.h;
+        cells += g.image ? nz + g.h : nz;
+        zs += nz;
+        uint32_t local = 0;
+        for (uint32_t k = 0; k < fd.ndraws; ++k) {
+            const uint32_t d = fd.first_draw + k;
+            const MeshView mv = sloth_mesh_view(b->meshes[d]);
+            BatchDraw &bd = hd[d];
+            bd.mesh = MeshDev{mv.x, mv.y, mv.z, mv.idx, mv.rgb, mv.nvert, mv.ntri};
+            bd.frame = f;
+            bd.rec_off = (uint32_t)(rec + local);
+            bd.local_base = local;
+            bd.vert_off = (uint32_t)vert;
+            for (uint32_t q = 0; q < (mv.nvert + 3) / 4; q += 256) bv.push_back(make_int2((int)d, (int)q));
+            for (uint32_t t = 0; t < mv.ntri; t += kBatchSetupBlock) bt.push_back(make_int2((int)d, (int)t));
+            if (g.image)
+                for (uint32_t t = 0; t < mv.ntri; t += kBatchNewlineChunk) bn.push_back(make_int2((int)d, (int)t));
+            local += mv.ntri;
+            vert += mv.nvert;
+        }
+        rec += local;
+        const uint64_t nc = g.image ? nz + g.h : nz;
+        for (uint64_t c = 0; c < nc; c += kBatchResolveChunk) br.push_back(make_int2((int)f, (int)c));
+    }
+    if (rec > 0x7fffffffull) return sloth_ctx_fail(b->ctx, SLOTH_ERR_LIMIT, "batch has more than 2^31 triangles");
+    tile_off[nf] = tiles;
+    b->cell_off[nf] = cells;
+    b->z_off[nf] = zs;
+    b->total_tiles = tiles;
+    b->total_cells = cells;
+    b->total_z = zs;
+    b->total_keys = keys;
+    b->total_nl = nl;
+    b->total_rec = rec;
+    b->total_vert = vert;
+
+    BCU(b, balloc(&b->tv, vert));
+    BCU(b, balloc(&b->records, rec));
+    BCU(b, balloc(&b->keys, keys));
+    BCU(b, balloc(&b->tile_gen, tiles));
+    BCU(b, balloc(&b->nltree, nl));
+    BCU(b, balloc(&b->z, zs));
+    BCU(b, balloc(&b->cells, cells));
+    BCU(b, balloc(&b->winner, zs));
+    BCU(b, balloc(&b->fragments, 1));
+    BCU(b, balloc(&b->frame_tile_off, nf + 1));
+    BCU(b, balloc(&b->bb.tile_count, tiles));
+    BCU(b, balloc(&b->bb.tile_offset, tiles + 1));
+    BCU(b, balloc(&b->bb.tile_cursor, tiles));
+    BCU(b, balloc(&b->bb.large_queue, rec));
+    BCU(b, balloc(&b->bb.large_count, 1));
+    BCU(b, balloc(&b->large_frame, rec));
+    BCU(b, balloc(&b->queue_head, 1));
+    BCU(b, balloc(&b->overflow, 1));
+    BCU(b, balloc(&b->d_mats, nd));
+    for (uint32_t f = 0; f < nf; ++f) {
+        BatchFrame &bf = b->hframes[f];
+        bf.fb.keys = b->keys + key_off[f];
+        bf.fb.tile_gen = b->tile_gen + tile_off[f];
+        bf.fb.nltree = b->nltree + nl_off[f];
+        bf.fb.records = b->records + rec_off[f];
+        bf.fb.z_out = b->z + b->z_off[f];
+        bf.fb.cells_out = b->cells + b->cell_off[f];
+        bf.fb.winner_out = b->winner + b->z_off[f];
+        bf.fb.fragments = b->fragments;
+        bf.fb.gen = 1;
+    }
+    BCU(b, balloc(&b->d_frames, nf));
+    BCU(b, balloc(&b->d_draws, nd));
+    BCU(b, cudaMemcpy(b->d_frames, b->hframes.data(), nf * sizeof(BatchFrame), cudaMemcpyHostToDevice));
+    BCU(b, cudaMemcpy(b->d_draws, hd.data(), nd * sizeof(BatchDraw), cudaMemcpyHostToDevice));
+    BCU(b, cudaMemcpy(b->frame_tile_off, tile_off.data(), (nf + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    std::vector<int2> *tabs[4] = {&bv, &bt, &bn, &br};
+    for (int i = 0; i < 4; ++i) {
+        b->nblk[i] = (uint32_t)tabs[i]->size();
+        BCU(b, balloc(&b->blk[i], tabs[i]->size()));
+        if (!tabs[i]->empty())
+            BCU(b, cudaMemcpy(b->blk[i], tabs[i]->data(), tabs[i]->size() * sizeof(int2), cudaMemcpyHostToDevice));
+    }
+    return SLOTH_OK;
+}
+
+BatchDev dev_view(sloth_batch *b)
+{
+    BatchDev d{};
+    d.frames = b->d_frames;
+    d.draws = b->d_draws;
+    d.mats = b->d_mats;
+    d.tv = b->tv;
+    d.nframes = (uint32_t)b->frames.size();
+    d.ndraws = (uint32_t)b->meshes.size();
+    d.total_tiles = b->total_tiles;
+    d.frame_tile_off = b->frame_tile_off;
+    d.bb = b->bb;
+    d.bb.capacity = (uint32_t)(b->entries_cap > 0xffffffffu ? 0xffffffffu : b->entries_cap);
+    d.large_frame = b->large_frame;
+    d.queue_head = b->queue_head;
+    d.overflow = b->overflow;
+    d.depth_cull = sloth_ctx_depth_cull(b->ctx);
+    return d;
+}
+
+// Stage 1: reset, matrices, vertices, setup, newline, large counts, scan.
+cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
+{
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(b->bb.tile_count, 0, (size_t)b->total_tiles * 4, s))) return e;
+    if ((e = cudaMemsetAsync(b->tile_gen, 0, (size_t)b->total_tiles * 4, s))) return e;
+    if ((e = cudaMemsetAsync(b->nltree, 0xff, (size_t)b->total_nl * 4, s))) return e;
+    if ((e = cudaMemsetAsync(b->bb.large_count, 0, 4, s))) return e;
+    if ((e = cudaMemsetAsync(b->fragments, 0, 8, s))) return e;
+    if ((e = cudaMemsetAsync(b->queue_head, 0, 4, s))) return e;
+    if ((e = cudaMemsetAsync(b->overflow, 0, 4, s))) return e;
+    if ((e = cudaMemcpyAsync(b->d_mats, b->h_mats, b->meshes.size() * sizeof(Mat4), cudaMemcpyHostToDevice, s)))
+        return e;
+    if ((e = launch_batch_vertex(d, b->blk[0], b->nblk[0], s))) return e;
+    if ((e = launch_batch_setup(d, b->blk[1], b->nblk[1], s))) return e;
+    if ((e = launch_batch_newline(d, b->blk[2], b->nblk[2], b->max_nl, s))) return e;
+    if ((e = launch_batch_bin_large(d, false, s))) return e;
+    return launch_bin_scan(b->total_tiles, d.bb, s);
+}
+
+// Stage 2: fill, persistent raster, resolve.
+cudaError_t enqueue_back(sloth_batch *b, const BatchDev &d, cudaStream_t s)
+{
+    cudaError_t e;
+    if ((e = launch_batch_fill(d, b->blk[1], b->nblk[1], s))) return e;
+    if ((e = launch_batch_bin_large(d, true, s))) return e;
+    const int tw = kTileShapes[b->shape][0], th = kTileShapes[b->shape][1];
+    if ((e = launch_batch_raster(d, tw, th, s))) return e;
+    return launch_batch_resolve(d, b->blk[3], b->nblk[3], s);
+}
+
+// Render without the graph: stage 1, size the entries from the scan total, stage 2.
+sloth_status render_planned(sloth_batch *b)
+{
+    cudaStream_t s = b->stream;
+    BatchDev d = dev_view(b);
+    BCU(b, enqueue_front(b, d, s));
+    BCU(b, cudaMemcpyAsync(b->h_total, b->bb.tile_offset + b->total_tiles, 4, cudaMemcpyDeviceToHost, s));
+    BCU(b, cudaStreamSynchronize(s));
+    const size_t need = (size_t)*b->h_total;
+    if (need > b->entries_cap || !b->bb.entries) {
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+        bfree(b->bb.entries);
+        const size_t cap = need + need / 4 + 1024;   // headroom for other transforms
+        BCU(b, balloc(&b->bb.entries, cap));
+        b->entries_cap = cap;
+        d = dev_view(b);
+    }
+    BCU(b, enqueue_back(b, d, s));
+    b->rendered = true;
+    return SLOTH_OK;
+}
+
+sloth_status capture(sloth_batch *b)
+{
+    cudaStream_t s = b->stream;
+    const BatchDev d = dev_view(b);
+    cudaGraph_t g = nullptr;
+    BCU(b, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue_front(b, d, s);
+    if (e == cudaSuccess) e = enqueue_back(b, d, s);
+    cudaError_t e2 = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return sloth_ctx_fail(b->ctx, SLOTH_ERR_CUDA, "batch graph capture failed");
+    }
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    BCU(b, e);
+    return SLOTH_OK;
+}
+
+// After a render: if the entries outgrew their buffer, re-plan and re-render.
+sloth_status settle(sloth_batch *b)
+{
+    BCU(b, cudaMemcpyAsync(b->h_overflow, b->overflow, 4, cudaMemcpyDeviceToHost, b->stream));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    if (*b->h_overflow) {
+        sloth_status st = render_planned(b);
+        if (st != SLOTH_OK) return st;
+        BCU(b, cudaStreamSynchronize(b->stream));
+    }
+    return SLOTH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+sloth_status sloth_batch_create(sloth_ctx *ctx, const sloth_frame_desc *frames, uint32_t nframes,
+                                const sloth_draw_desc *draws, uint32_t ndraws, sloth_batch **out)
+{
+    if (!ctx || !out || (nframes && !frames) || (ndraws && !draws)) return SLOTH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    for (uint32_t f = 0; f < nframes; ++f) {
+        const sloth_frame_desc &fd = frames[f];
+        if (fd.width < 1 || fd.height < 1 || fd.width > SLOTH_MAX_DIM || fd.height > SLOTH_MAX_DIM)
+            return sloth_ctx_fail(ctx, SLOTH_ERR_LIMIT, "frame viewport outside 1..65535");
+        if ((uint64_t)fd.first_draw + fd.ndraws > ndraws)
+            return sloth_ctx_fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "frame draws outside the draw array");
+        if (f > 0 && fd.first_draw != frames[f - 1].first_draw + frames[f - 1].ndraws)
+            return sloth_ctx_fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "frames must list consecutive draw ranges");
+    }
+    if (nframes && frames[0].first_draw != 0)
+        return sloth_ctx_fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "the first frame must start at draw 0");
+    const int dev = sloth_ctx_device(ctx);
+    for (uint32_t d = 0; d < ndraws; ++d) {
+        if (!draws[d].mesh) return sloth_ctx_fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "draw without a mesh");
+        if (sloth_mesh_view(draws[d].mesh).device != dev)
+            return sloth_ctx_fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "mesh on another device");
+    }
+    if (cudaSetDevice(dev) != cudaSuccess) return SLOTH_ERR_CUDA;
+    sloth_batch *b = new sloth_batch();
+    b->ctx = ctx;
+    b->device = dev;
+    b->stream = sloth_ctx_stream(ctx);
+    b->frames.assign(frames, frames + nframes);
+    for (uint32_t d = 0; d < ndraws; ++d) {
+        b->meshes.push_back(draws[d].mesh);
+        b->transforms.insert(b->transforms.end(), draws[d].transform, draws[d].transform + 16);
+    }
+    if (cudaMallocHost(&b->h_mats, (ndraws ? ndraws : 1) * sizeof(Mat4)) != cudaSuccess ||
+        cudaMallocHost(&b->h_total, 4) != cudaSuccess || cudaMallocHost(&b->h_overflow, 4) != cudaSuccess ||
+        prepare_batch_kernels() != cudaSuccess) {
+        sloth_batch_destroy(b);
+        return sloth_ctx_fail(ctx, SLOTH_ERR_OUT_OF_MEMORY, "batch host buffers");
+    }
+    set_mats(b);
+    const sloth_status st = build(b, 0);
+    if (st != SLOTH_OK) {
+        sloth_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return SLOTH_OK;
+}
+
+void sloth_batch_destroy(sloth_batch *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    free_layout(b);
+    if (b->h_mats) cudaFreeHost(b->h_mats);
+    if (b->h_total) cudaFreeHost(b->h_total);
+    if (b->h_overflow) cudaFreeHost(b->h_overflow);
+    delete b;
+}
+
+sloth_status sloth_batch_set_transforms(sloth_batch *b, const float *transforms)
+{
+    if (!b || !transforms) return SLOTH_ERR_INVALID_ARGUMENT;
+    BCU(b, cudaSetDevice(b->device));
+    BCU(b, cudaStreamSynchronize(b->stream));   // the previous render has read the matrices
+    memcpy(b->transforms.data(), transforms, b->transforms.size() * sizeof(float));
+    set_mats(b);
+    return SLOTH_OK;
+}
+
+sloth_status sloth_batch_render(sloth_batch *b)
+{
+    if (!b) return SLOTH_ERR_INVALID_ARGUMENT;
+    BCU(b, cudaSetDevice(b->device));
+    if (!b->rendered || !b->bb.entries) return render_planned(b);
+    if (!b->graph && b->stream != nullptr) {
+        const sloth_status st = capture(b);
+        if (st != SLOTH_OK) return st;
+    }
+    if (b->graph) {
+        BCU(b, cudaGraphLaunch(b->graph, b->stream));
+        return SLOTH_OK;
+    }
+    return render_planned(b);
+}
+
+sloth_status sloth_batch_read(sloth_batch *b, uint32_t frame, uint32_t *cells, float *z, int32_t *winner)
+{
+    if (!b || frame >= b->frames.size()) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b->rendered) return sloth_ctx_fail(b->ctx, SLOTH_ERR_INVALID_ARGUMENT, "render the batch first");
+    BCU(b, cudaSetDevice(b->device));
+    sloth_status st = settle(b);
+    if (st != SLOTH_OK) return st;
+    const uint64_t nc = b->cell_off[frame + 1] - b->cell_off[frame];
+    const uint64_t nz = b->z_off[frame + 1] - b->z_off[frame];
+    if (cells)
+        BCU(b, cudaMemcpyAsync(cells, b->cells + b->cell_off[frame], nc * 4, cudaMemcpyDeviceToHost, b->stream));
+    if (z) BCU(b, cudaMemcpyAsync(z, b->z + b->z_off[frame], nz * 4, cudaMemcpyDeviceToHost, b->stream));
+    if (winner)
+        BCU(b, cudaMemcpyAsync(winner, b->winner + b->z_off[frame], nz * 4, cudaMemcpyDeviceToHost, b->stream));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return SLOTH_OK;
+}
+
+sloth_status sloth_batch_frame_buffers(sloth_batch *b, uint32_t frame, const uint32_t **cells, const float **z)
+{
+    if (!b || frame >= b->frames.size()) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (cells) *cells = b->cells + b->cell_off[frame];
+    if (z) *z = b->z + b->z_off[frame];
+    return SLOTH_OK;
+}
+
+sloth_status sloth_batch_fragments(sloth_batch *b, uint64_t *fragments)
+{
+    if (!b || !fragments) return SLOTH_ERR_INVALID_ARGUMENT;
+    BCU(b, cudaSetDevice(b->device));
+    sloth_status st = settle(b);
+    if (st != SLOTH_OK) return st;
+    unsigned long long v = 0;
+    BCU(b, cudaMemcpy(&v, b->fragments, 8, cudaMemcpyDeviceToHost));
+    *fragments = v;
+    return SLOTH_OK;
+}
+
+sloth_status sloth_batch_set_tile_shape(sloth_batch *b, int shape)
+{
+    if (!b || shape < 0 || shape >= kNumTileShapes) return SLOTH_ERR_INVALID_ARGUMENT;
+    BCU(b, cudaSetDevice(b->device));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return shape == b->shape ? SLOTH_OK : build(b, shape);
+}
+
+sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, float *best_ms)
+{
+    if (!b) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (reps < 1) reps = 3;
+    BCU(b, cudaSetDevice(b->device));
+    cudaEvent_t e0, e1;
+    BCU(b, cudaEventCreate(&e0));
+    BCU(b, cudaEventCreate(&e1));
+    int best = -1;
+    float best_t = 0.0f;
+    for (int shape = 0; shape < kNumTileShapes; ++shape) {
+        sloth_status st = sloth_batch_set_tile_shape(b, shape);
+        if (st == SLOTH_OK) st = sloth_batch_render(b);     // plan + size the entries
+        if (st == SLOTH_OK) st = settle(b);
+        if (st == SLOTH_OK) st = sloth_batch_render(b);     // capture + warm
+        if (st != SLOTH_OK) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return st;
+        }
+        cudaEventRecord(e0, b->stream);
+        for (int i = 0; i < reps; ++i) sloth_batch_render(b);
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)reps;
+        if (best < 0 || ms < best_t) {
+            best = shape;
+            best_t = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sloth_status st = sloth_batch_set_tile_shape(b, best);
+    if (st != SLOTH_OK) return st;
+    if (best_shape) *best_shape = best;
+    if (best_ms) *best_ms = best_t;
+    return SLOTH_OK;
+}
+
+sloth_status sloth_tile_shape(int shape, uint32_t *cells, uint32_t *rows)
+{
+    if (shape < 0 || shape >= kNumTileShapes) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (cells) *cells = (uint32_t)kTileShapes[shape][0];
+    if (rows) *rows = (uint32_t)kTileShapes[shape][1];
+    return SLOTH_OK;
+}
+
+}  // extern "C"

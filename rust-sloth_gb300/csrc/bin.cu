@@ -1,32 +1,20 @@
-// bin.cu -- binning of triangles into target-cell tiles.
+// bin.cu -- binning of one frame's triangles into target-cell tiles.
 //
 // The reference visits every sample of every triangle's range in one sequential loop
 // (src/rasterizer.rs:69-70).  Here each triangle is listed in the tiles whose depth
 // cells it can write: count (setup kernel for small triangles, one warp per large
-// triangle here), exclusive scan over tiles, then fill.  A tile is listed only if the
-// exact corner test (rect_may_cover) cannot rule it out.  The order inside a tile list
-// does not matter: the raster's 64-bit atomicMin recovers the draw order.
-#include "bounds.cuh"
-#include "sloth_internal.cuh"
+// triangle here), exclusive scan over tiles, then fill (bin_common.cuh).
+#include "bin_common.cuh"
 #include "sloth_kernels.h"
 
 namespace sloth {
-
-// A tile entry: the ordered depth lower bound in the high word (the raster sorts on it,
-// front to back), the draw index in bits 0..30 and, in bit 31, whether the triangle has
-// wrapped samples in this tile (they write other cells than unwrapped samples).
-__device__ __forceinline__ uint64_t entry_key(float zlo, uint32_t gtri, bool wrapped)
-{
-    return ((uint64_t)ordered_z(zlo) << 32) | gtri | (wrapped ? 0x80000000u : 0u);
-}
 
 __device__ __forceinline__ Viewport vp_of(const FrameGeom &g)
 {
     return Viewport{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
 }
 
-// One warp per queued large triangle: lanes walk its tile rectangles (count or fill),
-// then its newline rows.
+// One warp per queued large triangle.
 template <bool kFill>
 __global__ void __launch_bounds__(256)
 bin_large_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
@@ -38,42 +26,8 @@ bin_large_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
     const Viewport vp = vp_of(g);
     for (uint32_t q = warp; q < nq; q += nwarps) {
         const uint32_t gtri = tri_base + bb.large_queue[q];
-        const TriRecord r = fb.records[gtri];
-        const TileSpan sp = tile_span(vp, r);
-        const OrientBound ob = orient_bound(r);
-        const int nu = (sp.TU.xb - sp.TU.xa) * (sp.TU.yb - sp.TU.ya);
-        const int nw = (sp.TW.xb - sp.TW.xa) * (sp.TW.yb - sp.TW.ya);
-        const int uw = sp.TU.xb - sp.TU.xa, ww = sp.TW.xb - sp.TW.xa;
-        for (int k = lane; k < nu + nw; k += 32) {
-            int tr, tc;
-            if (k < nu) {
-                tr = sp.TU.ya + k / uw;
-                tc = sp.TU.xa + k % uw;
-            } else {
-                tr = sp.TW.ya + (k - nu) / ww;
-                tc = sp.TW.xa + (k - nu) % ww;
-                if (in_rect(sp.TU, tr, tc)) continue;
-            }
-            if (!tile_hit(r, vp, sp.U, sp.W, tr, tc)) continue;
-            const uint32_t tile = tr * g.ntx + tc;
-            if (kFill) {
-                // depth bound of this triangle inside this tile (tighter than the
-                // triangle-wide bound for large triangles)
-                float zlo = r.zlo;
-                const Rect cu = sp.U.empty() ? Rect{0, 0, 0, 0} : clip_unwrapped(vp, sp.U, tr, tc);
-                const Rect cw = sp.W.empty() ? Rect{0, 0, 0, 0} : clip_wrapped(vp, sp.W, tr, tc);
-                if (r.flags & kFlagFiniteXY) {
-                    float zt = INFINITY;
-                    if (!cu.empty()) zt = fminf(zt, rect_depth_lower_bound(r, ob, cu));
-                    if (!cw.empty()) zt = fminf(zt, rect_depth_lower_bound(r, ob, cw));
-                    zlo = fmaxf(zlo, zt);
-                }
-                const uint32_t slot = atomicAdd(&bb.tile_cursor[tile], 1u);
-                if (slot < bb.capacity) bb.entries[slot] = entry_key(zlo, gtri, !cw.empty());
-            } else {
-                atomicAdd(&bb.tile_count[tile], 1u);
-            }
-        }
+        bin_large_warp<kFill>(fb.records[gtri], gtri, vp, bb.tile_count, bb.tile_cursor, bb.entries,
+                              bb.capacity, lane);
     }
 }
 
@@ -126,19 +80,7 @@ bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, 
     const Viewport vp = vp_of(g);
     const TileSpan sp = tile_span(vp, r);
     if (sp.large || sp.ntiles == 0) return;
-    auto put = [&](int tr, int tc) {
-        const bool wrapped = !sp.W.empty() && !clip_wrapped(vp, sp.W, tr, tc).empty();
-        const uint32_t slot = atomicAdd(&bb.tile_cursor[tr * g.ntx + tc], 1u);
-        if (slot < bb.capacity) bb.entries[slot] = entry_key(r.zlo, gtri, wrapped);
-    };
-    for (int tr = sp.TU.ya; tr < sp.TU.yb; ++tr)
-        for (int tc = sp.TU.xa; tc < sp.TU.xb; ++tc)
-            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
-    for (int tr = sp.TW.ya; tr < sp.TW.yb; ++tr)
-        for (int tc = sp.TW.xa; tc < sp.TW.xb; ++tc) {
-            if (in_rect(sp.TU, tr, tc)) continue;
-            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
-        }
+    fill_small(r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
 }
 
 static int large_grid()

@@ -1,0 +1,82 @@
+// bin_common.cuh -- per-triangle binning steps shared by the single-frame and batched
+// kernels.  A triangle is listed in every target-cell tile whose cells it can write
+// (tile_hit: an exact corner test cannot rule the tile out).  The order inside a tile
+// list does not matter: the raster's 64-bit atomicMin recovers the draw order.
+#pragma once
+
+#include "bounds.cuh"
+#include "sloth_internal.cuh"
+
+namespace sloth {
+
+// A tile entry: the ordered depth lower bound in the high word (the raster sorts on it,
+// front to back), the draw index in bits 0..30 and, in bit 31, whether the triangle has
+// wrapped samples in this tile (they write other cells than unwrapped samples).
+__device__ __forceinline__ uint64_t entry_key(float zlo, uint32_t gtri, bool wrapped)
+{
+    return ((uint64_t)ordered_z(zlo) << 32) | gtri | (wrapped ? 0x80000000u : 0u);
+}
+
+// One warp walks a large triangle's tile rectangles: counts (kFill false) or writes its
+// entries (kFill true), with a per-tile depth bound (tighter than the triangle-wide one).
+template <bool kFill>
+__device__ __forceinline__ void bin_large_warp(const TriRecord &r, uint32_t gtri, const Viewport &vp,
+                                               uint32_t *tile_count, uint32_t *tile_cursor,
+                                               uint64_t *entries, uint32_t capacity, int lane)
+{
+    const TileSpan sp = tile_span(vp, r);
+    const OrientBound ob = orient_bound(r);
+    const int nu = (sp.TU.xb - sp.TU.xa) * (sp.TU.yb - sp.TU.ya);
+    const int nw = (sp.TW.xb - sp.TW.xa) * (sp.TW.yb - sp.TW.ya);
+    const int uw = sp.TU.xb - sp.TU.xa, ww = sp.TW.xb - sp.TW.xa;
+    for (int k = lane; k < nu + nw; k += 32) {
+        int tr, tc;
+        if (k < nu) {
+            tr = sp.TU.ya + k / uw;
+            tc = sp.TU.xa + k % uw;
+        } else {
+            tr = sp.TW.ya + (k - nu) / ww;
+            tc = sp.TW.xa + (k - nu) % ww;
+            if (in_rect(sp.TU, tr, tc)) continue;
+        }
+        if (!tile_hit(r, vp, sp.U, sp.W, tr, tc)) continue;
+        const uint32_t tile = tr * vp.ntx + tc;
+        if (kFill) {
+            float zlo = r.zlo;
+            const Rect cu = sp.U.empty() ? Rect{0, 0, 0, 0} : clip_unwrapped(vp, sp.U, tr, tc);
+            const Rect cw = sp.W.empty() ? Rect{0, 0, 0, 0} : clip_wrapped(vp, sp.W, tr, tc);
+            if (r.flags & kFlagFiniteXY) {
+                float zt = INFINITY;
+                if (!cu.empty()) zt = fminf(zt, rect_depth_lower_bound(r, ob, cu));
+                if (!cw.empty()) zt = fminf(zt, rect_depth_lower_bound(r, ob, cw));
+                zlo = fmaxf(zlo, zt);
+            }
+            const uint32_t slot = atomicAdd(&tile_cursor[tile], 1u);
+            if (slot < capacity) entries[slot] = entry_key(zlo, gtri, !cw.empty());
+        } else {
+            atomicAdd(&tile_count[tile], 1u);
+        }
+    }
+}
+
+// One thread writes a small triangle's entries.
+__device__ __forceinline__ void fill_small(const TriRecord &r, uint32_t gtri, const Viewport &vp,
+                                           const TileSpan &sp, uint32_t *tile_cursor, uint64_t *entries,
+                                           uint32_t capacity)
+{
+    auto put = [&](int tr, int tc) {
+        const bool wrapped = !sp.W.empty() && !clip_wrapped(vp, sp.W, tr, tc).empty();
+        const uint32_t slot = atomicAdd(&tile_cursor[tr * vp.ntx + tc], 1u);
+        if (slot < capacity) entries[slot] = entry_key(r.zlo, gtri, wrapped);
+    };
+    for (int tr = sp.TU.ya; tr < sp.TU.yb; ++tr)
+        for (int tc = sp.TU.xa; tc < sp.TU.xb; ++tc)
+            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
+    for (int tr = sp.TW.ya; tr < sp.TW.yb; ++tr)
+        for (int tc = sp.TW.xa; tc < sp.TW.xb; ++tc) {
+            if (in_rect(sp.TU, tr, tc)) continue;
+            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
+        }
+}
+
+}  // namespace sloth

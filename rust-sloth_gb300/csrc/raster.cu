@@ -1,196 +1,18 @@
-// raster.cu -- per-tile rasterization with a shared-memory depth-key tile.
-//
-// Replaces the sample loop of src/rasterizer.rs:69-86.  One CTA owns one tile of depth
-// cells (kTileH rows x kTileW cells).  Its warps take the tile's triangle entries one at
-// a time; the 32 lanes walk the triangle's samples inside the tile (unwrapped and wrapped
-// parts), evaluate the three edge functions and the barycentric depth in the reference's
-// f32 operation order, and fold (depth, draw index) keys into the tile with a 64-bit
-// shared-memory atomicMin.  The minimum key of a cell is the reference's last successful
-// depth write.  Keys of earlier draws since the clear are merged in first.
-//
-// Depth culling (on by default): entries carry a proven lower bound of every depth their
-// triangle can produce in this tile (bounds.cuh).  The CTA sorts its entries on that
-// bound (front to back) and keeps an upper bound of the farthest key depth among the
-// tile's writable cells.  An entry whose bound is strictly above it cannot win any cell,
-// and neither can the entries sorted after it, so the warps stop there.  Only skipped
-// work changes: the buffers are the same bit for bit; the fragment counter then counts
-// only the fragments of the triangles that were rasterized.
-#include "sloth_internal.cuh"
-#include "sloth_kernels.h"
+// raster.cu -- per-tile rasterization of one frame (raster_common.cuh), one CTA per tile,
+// instantiated for every supported tile shape.
+#include "raster_common.cuh"
 
 namespace sloth {
 
-constexpr int TW = kTileW, TH = kTileH;
-constexpr int kSortCap = 2048;   // entries sorted per pass (16 KB of shared memory)
-
-__device__ __forceinline__ TriRecord load_record(const TriRecord *__restrict__ recs, uint32_t i)
-{
-    const float4 *p = reinterpret_cast<const float4 *>(recs + i);
-    TriRecord r;
-    float4 *o = reinterpret_cast<float4 *>(&r);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) o[k] = __ldg(p + k);
-    return r;
-}
-
-// Walk the samples of rect c (row-major, 32 at a time) and fold covered samples' keys.
-template <int kNotWrapped>
-__device__ __forceinline__ void raster_part(const TriRecord &r, uint32_t gtri, Rect c, int R0,
-                                            int C0, int w, unsigned long long *skeys, int lane,
-                                            uint32_t &frags)
-{
-    if (c.empty()) return;
-    if ((r.flags & kFlagFiniteXY) && !rect_may_cover(r, c)) return;
-    const int bw = c.xb - c.xa;
-    const int area = bw * (c.yb - c.ya);
-    const int q = 32 / bw, rem = 32 - q * bw;
-    int dx = lane % bw, dy = lane / bw;
-    for (int k = lane; k < area; k += 32) {
-        const int x = c.xa + dx, y = c.ya + dy;
-        const float px = (float)x, py = (float)y;
-        const EdgeVals e = eval_edges(r, px, py);
-        if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
-            ++frags;
-            const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
-            if (z < kFltMax) {
-                const unsigned long long key = make_key(z, gtri, kNotWrapped);
-                const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
-                const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
-                unsigned long long *p = &skeys[row * TW + col];
-                if (key < *(volatile unsigned long long *)p) atomicMin(p, key);
-            }
-        }
-        dx += rem;
-        dy += q;
-        if (dx >= bw) {
-            dx -= bw;
-            ++dy;
-        }
-    }
-}
-
-// Upper bounds of the farthest depth (ordered high key word) among the tile's cells that
-// unwrapped samples can write (row y in [1,h-2], column 2x in [2,w-1], even) and among
-// those wrapped samples can write (row y+1 in [2,h-1], column 2x-w in [0,w-4], of the
-// parity of w).  Reads race with the atomics of other warps; key values only decrease, so
-// the results stay upper bounds of every later state.
-__device__ __forceinline__ void tile_zmax(const unsigned long long *skeys, int R0, int C0,
-                                          const FrameGeom &g, int lane, uint32_t &mu, uint32_t &mw)
-{
-    mu = 0;
-    mw = 0;
-    const int wpar = g.w & 1;
-    for (int i = lane; i < TH * TW; i += 32) {
-        const int row = i / TW, col = i - row * TW;
-        const int gr = R0 + row, gc = C0 + col;
-        const uint32_t v = (uint32_t)(*(volatile const unsigned long long *)&skeys[i] >> 32);
-        if (gr >= 1 && gr <= g.h - 2 && gc >= 2 && gc <= g.w - 1 && (gc & 1) == 0) mu = max(mu, v);
-        if (gr >= 2 && gr <= g.h - 1 && gc <= g.w - 4 && (gc & 1) == wpar) mw = max(mw, v);
-    }
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        mu = max(mu, __shfl_xor_sync(0xffffffffu, mu, d));
-        mw = max(mw, __shfl_xor_sync(0xffffffffu, mw, d));
-    }
-}
-
-__global__ void __launch_bounds__(256)
+template <int TW, int TH>
+__global__ void __launch_bounds__(kRasterThreads)
 raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb, int depth_cull)
 {
-    __shared__ unsigned long long skeys[TH * TW];
-    __shared__ unsigned long long sent[kSortCap];
-    __shared__ uint32_t s_next, s_zmax_u, s_zmax_w;
-    __shared__ uint32_t s_frags[8];
+    __shared__ TileSmem<TW, TH> S;
     const int tile = blockIdx.x;
     const uint32_t cnt = bb.tile_count[tile];
     if (cnt == 0) return;
-    const uint32_t off = bb.tile_offset[tile];
-    const int tr = tile / g.ntx, tc = tile - (tile / g.ntx) * g.ntx;
-    const int R0 = tr * TH, C0 = tc * TW;
-    const bool merge = fb.tile_gen[tile] == fb.gen;
-    unsigned long long *gk = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)R0 * g.pitch + C0;
-    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
-        const int rr = i / TW, cc = i - rr * TW;
-        skeys[i] = merge ? gk[(size_t)rr * g.pitch + cc] : kEmptyKey;
-    }
-    if (threadIdx.x == 0) s_zmax_u = s_zmax_w = 0xffffffffu;
-
-    const int lane = threadIdx.x & 31;
-    const Viewport vp{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
-    uint32_t frags = 0;
-    for (uint32_t base = 0; base < cnt; base += kSortCap) {
-        const uint32_t n = min(cnt - base, (uint32_t)kSortCap);
-        uint32_t np2 = 2;
-        while (np2 < n) np2 <<= 1;
-        for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x)
-            sent[i] = i < n ? bb.entries[off + base + i] : ~0ull;
-        if (threadIdx.x == 0) s_next = 0;
-        __syncthreads();
-        if (depth_cull) {
-            // bitonic sort, ascending: front-to-back depth bounds
-            for (uint32_t k = 2; k <= np2; k <<= 1)
-                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                    for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) {
-                        const uint32_t ixj = i ^ j;
-                        if (ixj > i) {
-                            const unsigned long long a = sent[i], b = sent[ixj];
-                            if ((a > b) == ((i & k) == 0)) {
-                                sent[i] = b;
-                                sent[ixj] = a;
-                            }
-                        }
-                    }
-                    __syncthreads();
-                }
-        }
-        for (;;) {
-            uint32_t e = 0;
-            if (lane == 0) e = atomicAdd(&s_next, 1u);
-            e = __shfl_sync(0xffffffffu, e, 0);
-            if (e >= n) break;
-            const unsigned long long ent = sent[e];
-            if (depth_cull) {
-                if ((e & 15) == 15) {
-                    uint32_t mu, mw;
-                    tile_zmax(skeys, R0, C0, g, lane, mu, mw);
-                    if (lane == 0) {
-                        atomicMin(&s_zmax_u, mu);
-                        atomicMin(&s_zmax_w, mw);
-                    }
-                }
-                const uint32_t zlo = (uint32_t)(ent >> 32);
-                const uint32_t zu = *(volatile uint32_t *)&s_zmax_u, zw = *(volatile uint32_t *)&s_zmax_w;
-                const uint32_t lim = ((uint32_t)ent & 0x80000000u) ? max(zu, zw) : zu;
-                if (zlo > lim) {
-                    // sorted: every later entry is behind every writable cell too
-                    if (zlo > max(zu, zw)) break;
-                    continue;
-                }
-            }
-            const uint32_t gtri = (uint32_t)ent & 0x7fffffffu;
-            const TriRecord r = load_record(fb.records, gtri);
-            const Rect U = unwrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
-            if (!U.empty()) raster_part<1>(r, gtri, clip_unwrapped(vp, U, tr, tc), R0, C0, g.w, skeys, lane, frags);
-            const Rect W = wrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
-            if (!W.empty()) raster_part<0>(r, gtri, clip_wrapped(vp, W, tr, tc), R0, C0, g.w, skeys, lane, frags);
-        }
-        __syncthreads();
-    }
-    // fragment count: warp reduce, then one atomic per CTA
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) frags += __shfl_xor_sync(0xffffffffu, frags, d);
-    if (lane == 0) s_frags[threadIdx.x >> 5] = frags;
-    __syncthreads();
-    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
-        const int rr = i / TW, cc = i - rr * TW;
-        gk[(size_t)rr * g.pitch + cc] = skeys[i];
-    }
-    if (threadIdx.x == 0) {
-        uint32_t tot = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) tot += s_frags[k];
-        atomicAdd(fb.fragments, (unsigned long long)tot);
-        fb.tile_gen[tile] = fb.gen;
-    }
+    raster_tile<TW, TH>(S, g, fb, tile, cnt, bb.entries + bb.tile_offset[tile], depth_cull);
 }
 
 cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
@@ -198,8 +20,14 @@ cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinB
 {
     const int ntiles = g.ntx * g.nty;
     if (ntiles == 0) return cudaSuccess;
-    raster_kernel<<<ntiles, 256, 0, s>>>(g, fb, bb, depth_cull);
-    return cudaGetLastError();
+#define SLOTH_RASTER_CASE(W_, H_)                                                              \
+    if (g.tw == W_ && g.th == H_) {                                                            \
+        raster_kernel<W_, H_><<<ntiles, kRasterThreads, 0, s>>>(g, fb, bb, depth_cull);        \
+        return cudaGetLastError();                                                             \
+    }
+    SLOTH_TILE_SHAPES(SLOTH_RASTER_CASE)
+#undef SLOTH_RASTER_CASE
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace sloth

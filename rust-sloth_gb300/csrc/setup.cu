@@ -4,22 +4,11 @@
 // a = 1/orient) and src/geometry.rs:37-56 (Triangle::mul/aabb/normal).  The reference
 // recomputes utransform*transform per triangle and normal() per covered sample; both
 // are the same value every time, so they are formed once (matrix on the host, normal
-// here) with the same operation order.
-#include "bounds.cuh"
-#include "sloth_internal.cuh"
+// here) with the same operation order (record.cuh).
+#include "record.cuh"
 #include "sloth_kernels.h"
 
 namespace sloth {
-
-// nalgebra Matrix4*Vector4 with w = 1: ((m0*x + m1*y) + m2*z) + m3*1, each step rounded.
-__device__ __forceinline__ float row_dot(const float *m, float x, float y, float z)
-{
-    float acc = fmul(m[0], x);
-    acc = fadd(fmul(m[1], y), acc);
-    acc = fadd(fmul(m[2], z), acc);
-    acc = fadd(fmul(m[3], 1.0f), acc);
-    return acc;
-}
 
 // Four vertices per thread: float4 loads of the x, y and z arrays (structure of arrays).
 __global__ void __launch_bounds__(256) vertex_transform_kernel(MeshDev mesh, Mat4 M, float4 *tv)
@@ -55,64 +44,6 @@ __global__ void __launch_bounds__(256) vertex_transform_kernel(MeshDev mesh, Mat
     }
 }
 
-// Smallest index in [lo,hi) where a monotone (false..true) predicate holds, hi if none.
-template <class Pred>
-__device__ __forceinline__ int first_true(int lo, int hi, Pred pred)
-{
-    while (lo < hi) {
-        int mid = lo + ((hi - lo) >> 1);
-        if (pred(mid)) hi = mid;
-        else lo = mid + 1;
-    }
-    return lo;
-}
-
-// True if no sample (px >= X, py in [y0,y1)) can be covered.  Along a row, an edge with
-// dy > 0 is non-increasing in px and an edge with dy == 0 is constant, so if it is
-// negative at X it stays negative for all px >= X.  At column X, each such edge is
-// monotone in py (through C(py) = dx*(py-ay)), so the rows where it is negative form a
-// prefix or a suffix of [y0,y1); the rows are all excluded iff those sets cover [y0,y1).
-// Exact for records whose x,y are finite and below 1e18 (no overflow, no NaN).
-__device__ bool right_of_is_empty(const TriRecord &r, int X, int y0, int y1)
-{
-    const float px = (float)X;
-    int prefix_end = y0;     // max end of negative prefixes
-    int suffix_begin = y1;   // min begin of negative suffixes
-    const float dxs[3] = {r.dx0, r.dx1, r.dx2};
-    const float dys[3] = {r.dy0, r.dy1, r.dy2};
-    const float axs[3] = {r.v2x, r.v3x, r.v1x};
-    const float ays[3] = {r.v2y, r.v3y, r.v1y};
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const float dx = dxs[i], dy = dys[i], ax = axs[i], ay = ays[i];
-        if (!(dy >= 0.0f)) continue;   // dy < 0: the edge grows with px, proves nothing
-        auto neg = [&](int py) { return edge_eval(dx, dy, ax, ay, px, (float)py) < 0.0f; };
-        if (dx > 0.0f) {
-            // increasing in py: negative on a prefix
-            int b = first_true(y0, y1, [&](int py) { return !neg(py); });
-            prefix_end = max(prefix_end, b);
-        } else if (dx < 0.0f) {
-            // decreasing in py: negative on a suffix
-            int s = first_true(y0, y1, [&](int py) { return neg(py); });
-            suffix_begin = min(suffix_begin, s);
-        } else {
-            if (neg(y0)) return true;   // constant in py too
-        }
-    }
-    return prefix_end >= suffix_begin;
-}
-
-__device__ __forceinline__ int sat_lo(float f, int cap)
-{
-    // Rust `f as usize` of ceil(max(v,1.0)) (>= 1, never NaN), clamped to cap.
-    return f < (float)cap ? (int)f : cap;
-}
-__device__ __forceinline__ int sat_hi(float f)
-{
-    // Rust `f as usize` of ceil(min(v, dim-1)): NaN/negative -> 0, at most dim-1.
-    return f > 0.0f ? (int)f : 0;
-}
-
 __device__ __forceinline__ Viewport to_vp(const FrameGeom &g)
 {
     return Viewport{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
@@ -134,80 +65,14 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, Fra
         } else {
             i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
         }
-        const float4 p1 = __ldg(tv + i1), p2 = __ldg(tv + i2), p3 = __ldg(tv + i3);
-        TriRecord r;
-        r.v1x = p1.x; r.v1y = p1.y; r.v2x = p2.x; r.v2y = p2.y; r.v3x = p3.x; r.v3y = p3.y;
-        r.dx0 = fsub(p3.x, p2.x); r.dy0 = fsub(p3.y, p2.y);
-        r.dx1 = fsub(p1.x, p3.x); r.dy1 = fsub(p1.y, p3.y);
-        r.dx2 = fsub(p2.x, p1.x); r.dy2 = fsub(p2.y, p1.y);
-        r.v1z = p1.z; r.dz2 = fsub(p2.z, p1.z); r.dz3 = fsub(p3.z, p1.z);
-        // a = 1 / orient(v1, v2, v3)  (src/rasterizer.rs:67)
-        const float orient = edge_eval(r.dx2, r.dy2, p1.x, p1.y, p3.x, p3.y);
-        r.a = __fdiv_rn(1.0f, orient);
-        // normal().z  (src/geometry.rs:49-56; norm of a 4-vector with w = 0)
-        const float e1x = r.dx2, e1y = r.dy2, e1z = r.dz2;
-        const float e2x = fsub(p3.x, p1.x), e2y = fsub(p3.y, p1.y), e2z = r.dz3;
-        const float nx = fsub(fmul(e1y, e2z), fmul(e1z, e2y));
-        const float ny = fsub(fmul(e1z, e2x), fmul(e1x, e2z));
-        const float nz = fsub(fmul(e1x, e2y), fmul(e1y, e2x));
-        const float norm2 = fadd(fadd(fmul(nx, nx), fmul(nz, nz)), fadd(fmul(ny, ny), fmul(0.0f, 0.0f)));
-        const float n = __fsqrt_rn(fadd(0.0f, norm2));
-        r.na = fmul(__fdiv_rn(nz, n), r.a);
-        const uint8_t *c = mesh.rgb + 3 * (size_t)t;
-        r.rgb = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16);
-        // aabb and sample range  (src/geometry.rs:37-42, src/rasterizer.rs:59-66)
-        const float mnx = fminf(p1.x, fminf(p2.x, p3.x)), mny = fminf(p1.y, fminf(p2.y, p3.y));
-        const float mxx = fmaxf(p1.x, fmaxf(p2.x, p3.x)), mxy = fmaxf(p1.y, fmaxf(p2.y, p3.y));
-        r.x0 = sat_lo(ceilf(fmaxf(mnx, 1.0f)), g.w);
-        r.y0 = sat_lo(ceilf(fmaxf(mny, 1.0f)), g.h);
-        const int x1 = sat_hi(ceilf(fminf(fmul(mxx, 2.0f), (float)(g.w - 1))));
-        r.y1 = sat_hi(ceilf(fminf(mxy, (float)(g.h - 1))));
-        const float big = 1e18f;
-        const bool finite = fabsf(p1.x) < big && fabsf(p1.y) < big && fabsf(p2.x) < big &&
-                            fabsf(p2.y) < big && fabsf(p3.x) < big && fabsf(p3.y) < big;
-        r.flags = finite ? kFlagFiniteXY : 0u;
-        r.xe = x1;
-        r.zlo = -INFINITY;
-        if (finite && r.x0 < x1 && r.y0 < r.y1) {
-            // first column strictly right of the triangle, not left of x0
-            const float xf = fadd(floorf(mxx), 1.0f);
-            if (xf < (float)x1) {
-                const int X = xf <= (float)r.x0 ? r.x0 : (int)xf;
-                if (right_of_is_empty(r, X, r.y0, r.y1)) {
-                    r.xe = X;
-                    r.flags |= kFlagTight;
-                }
-            }
-            // cull triangles that provably cover no sample of the evaluated range (the
-            // range right of xe is already proven empty, or xe is the reference's bound)
-            if (r.x0 < r.xe) {
-                const OrientBound ob = orient_bound(r);
-                if (provably_empty(ob)) {
-                    r.xe = r.x0;
-                    r.flags |= kFlagCulled;
-                } else {
-                    r.zlo = depth_lower_bound(r, ob);
-                }
-            }
-        }
-        const uint32_t gtri = tri_base + t;
-        fb.records[gtri] = r;
-
+        const TriRecord r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3),
+                                         mesh.rgb + 3 * (size_t)t, g.w, g.h);
+        fb.records[tri_base + t] = r;
         // binning: count tiles of small triangles here, queue the rest for warps
         const Viewport vp = to_vp(g);
         const TileSpan sp = tile_span(vp, r);
-        const Rect &U = sp.U, &W = sp.W, &TU = sp.TU, &TW = sp.TW;
         large = sp.large;
-        if (!large) {
-            for (int tr = TU.ya; tr < TU.yb; ++tr)
-                for (int tc = TU.xa; tc < TU.xb; ++tc)
-                    if (tile_hit(r, vp, U, W, tr, tc)) atomicAdd(&bb.tile_count[tr * g.ntx + tc], 1u);
-            for (int tr = TW.ya; tr < TW.yb; ++tr)
-                for (int tc = TW.xa; tc < TW.xb; ++tc) {
-                    if (tr >= TU.ya && tr < TU.yb && tc >= TU.xa && tc < TU.xb) continue;
-                    if (tile_hit(r, vp, U, W, tr, tc)) atomicAdd(&bb.tile_count[tr * g.ntx + tc], 1u);
-                }
-        }
+        if (!large) count_small_tiles(r, vp, sp, bb.tile_count);
     }
     // warp-ballot compaction of the large-triangle queue
     const unsigned m = __ballot_sync(0xffffffffu, large);
@@ -242,19 +107,7 @@ newline_kernel(uint32_t ntri, uint32_t tri_base, uint32_t chunk, FrameGeom g, Fr
     for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
         const int32_t v = (int32_t)(tri_base + t);
         const int4 yr = __ldg(reinterpret_cast<const int4 *>(fb.records + tri_base + t) + 4);
-        int l = yr.z + n, r = yr.w + n;   // [y0, y1)
-        while (l < r) {
-            if (l & 1) {
-                if (kShared || *(volatile int32_t *)&tree[l] < v) atomicMax(&tree[l], v);
-                ++l;
-            }
-            if (r & 1) {
-                --r;
-                if (kShared || *(volatile int32_t *)&tree[r] < v) atomicMax(&tree[r], v);
-            }
-            l >>= 1;
-            r >>= 1;
-        }
+        nltree_update(tree, n, yr.z, yr.w, v, kShared);
     }
     if (kShared) {
         __syncthreads();

@@ -73,6 +73,7 @@ struct sloth_ctx {
 
     // instrumentation
     int depth_cull = 1;
+    int tile_shape = 0;
     bool timing = false;
     std::map<std::string, KernelClock> clocks;
     uint64_t launches = 0;
@@ -167,8 +168,8 @@ static sloth_status alloc_frame(sloth_ctx *ctx)
     g.w = (int32_t)ctx->req_w;
     g.h = (int32_t)ctx->req_h;
     g.image = ctx->req_image ? 1 : 0;
-    g.tw = kTileW;
-    g.th = kTileH;
+    g.tw = kTileShapes[ctx->tile_shape][0];
+    g.th = kTileShapes[ctx->tile_shape][1];
     g.ntx = (g.w + g.tw - 1) / g.tw;
     g.nty = (g.h + g.th - 1) / g.th;
     g.pitch = g.ntx * g.tw;
@@ -233,6 +234,25 @@ static sloth_status resolve_pending(sloth_ctx *ctx)
     CU(ctx, timed(ctx, "resolve", [&] { return launch_resolve(ctx->g, ctx->fb, ctx->stream); }));
     ctx->dirty = false;
     return SLOTH_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// accessors for the batch API (batch_api.cu)
+// ---------------------------------------------------------------------------------------
+sloth_status sloth_ctx_fail(sloth_ctx *ctx, sloth_status st, const char *msg) { return fail(ctx, st, "%s", msg); }
+int sloth_ctx_device(const sloth_ctx *ctx) { return ctx->device; }
+cudaStream_t sloth_ctx_stream(const sloth_ctx *ctx) { return ctx->stream; }
+int sloth_ctx_depth_cull(const sloth_ctx *ctx) { return ctx->depth_cull; }
+struct MeshView {
+    const float *x, *y, *z;
+    const uint32_t *idx;
+    const uint8_t *rgb;
+    uint32_t nvert, ntri;
+    int device;
+};
+MeshView sloth_mesh_view(const sloth_mesh *m)
+{
+    return MeshView{m->x, m->y, m->z, m->idx, m->rgb, m->nvert, m->ntri, m->device};
 }
 
 // ---------------------------------------------------------------------------------------
@@ -406,7 +426,8 @@ sloth_status sloth_ctx_clear(sloth_ctx *ctx)
         return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "no viewport: call sloth_ctx_set_viewport first");
     CU(ctx, cudaSetDevice(ctx->device));
     if (!ctx->have_frame || ctx->g.w != (int32_t)ctx->req_w || ctx->g.h != (int32_t)ctx->req_h ||
-        ctx->g.image != ctx->req_image) {
+        ctx->g.image != ctx->req_image || ctx->g.tw != kTileShapes[ctx->tile_shape][0] ||
+        ctx->g.th != kTileShapes[ctx->tile_shape][1]) {
         sloth_status st = alloc_frame(ctx);
         if (st != SLOTH_OK) return st;
     }
@@ -630,6 +651,10 @@ sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value)
 {
     if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
     switch (option) {
+    case SLOTH_OPTION_TILE_SHAPE:
+        if (value < 0 || value >= kNumTileShapes) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "no tile shape %lld", (long long)value);
+        ctx->tile_shape = (int)value;
+        return SLOTH_OK;
     case SLOTH_OPTION_DEPTH_CULL:
         if (value != 0 && value != 1) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "depth cull is 0 or 1");
         ctx->depth_cull = (int)value;

@@ -237,4 +237,32 @@ __device__ __forceinline__ bool in_rect(const Rect &t, int tr, int tc)
     return tr >= t.ya && tr < t.yb && tc >= t.xa && tc < t.xb;
 }
 
+// Newline segment tree over n (power of two) rows: fold draw index v into the rows
+// [y0,y1) with the canonical O(log n) node decomposition.  `always` forces the atomic
+// (shared-memory trees); otherwise a read filters updates that cannot raise a node.
+__device__ __forceinline__ void nltree_update(int32_t *tree, int n, int y0, int y1, int32_t v, bool always)
+{
+    int l = y0 + n, r = y1 + n;
+    while (l < r) {
+        if (l & 1) {
+            if (always || *(volatile int32_t *)&tree[l] < v) atomicMax(&tree[l], v);
+            ++l;
+        }
+        if (r & 1) {
+            --r;
+            if (always || *(volatile int32_t *)&tree[r] < v) atomicMax(&tree[r], v);
+        }
+        l >>= 1;
+        r >>= 1;
+    }
+}
+
+// The last newline writer of row y: the maximum over the leaf-to-root path (-1: none).
+__device__ __forceinline__ int32_t nltree_query(const int32_t *tree, int n, int y)
+{
+    int32_t t = -1;
+    for (uint32_t i = (uint32_t)y + (uint32_t)n; i >= 1; i >>= 1) t = max(t, tree[i]);
+    return t;
+}
+
 }  // namespace sloth

@@ -81,8 +81,13 @@ cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinB
 // resolve: keys -> z, frame cells, winners.
 cudaError_t launch_resolve(const FrameGeom &g, const FrameBuffers &fb, cudaStream_t s);
 
-constexpr int kTileW = 64;   // cells (even)
+constexpr int kTileW = 64;   // default tile: cells (even)
 constexpr int kTileH = 32;   // rows
+
+// Tile shapes the raster is compiled for, (cells, rows); the autotuner picks among them.
+#define SLOTH_TILE_SHAPES(X) X(64, 32) X(32, 16) X(64, 16) X(32, 32) X(128, 16)
+constexpr int kNumTileShapes = 5;
+constexpr int kTileShapes[kNumTileShapes][2] = {{64, 32}, {32, 16}, {64, 16}, {32, 32}, {128, 16}};
 constexpr uint32_t kSmallMaxTiles = 8;   // triangles over more tiles are binned by warps
 
 }  // namespace sloth
