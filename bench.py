@@ -337,6 +337,10 @@ def run_gpu(args):
                "sample": f"every {args.cpu_sample_den}th triangle of the frame ({n} triangles, 1/{args.cpu_sample_den} "
                          f"of the work) on one thread in {t:.2f} s; frames/s = 1/(den * time)"}
 
+    batched = None
+    if not args.no_batched:
+        batched = run_config3(torch, stream, local, args)
+
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -349,12 +353,116 @@ def run_gpu(args):
         "depth_cull": not args.no_depth_cull,
         "e2e": e2e,
         "gpu_launches": launches, "kernels": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+CONFIG3 = ("config3: 256 views of a displaced icosphere (subdivision 6, 81,920 triangles) at 640x360 "
+           "+ 64 soups with log-uniform triangle counts 1k-500k at viewports 80x24..1920x1080, image mode")
+
+
+def config3_frames(seed: int = 3):
+    """Host meshes and frame specs of config 3 (one mesh per frame)."""
+    import workloads as W
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    ico = W.displaced_icosphere(6, seed=seed, amplitude=0.1)
+    meshes = [ico]
+    frames = []
+    ext = O.scene_extent([ico["bbox_max"]])
+    for _ in range(256):
+        theta = float(rng.uniform(0.0, 2.0 * np.pi))
+        R = O.euler_rotation(*W.cli_rotation(pitch=theta))     # turntable axis
+        frames.append((0, 640, 360, True, O.viewport_transform(640, 360, ext), R))
+    sizes = [(80, 24), (160, 48), (640, 360), (1920, 1080)]
+    counts = np.exp(rng.uniform(np.log(1e3), np.log(5e5), size=64)).astype(int)
+    for i, n in enumerate(counts):
+        m = W.soup(int(n), seed=1000 + i, n_large=max(1, int(n) // 500))
+        meshes.append(m)
+        w, h = sizes[int(rng.integers(0, 4))]
+        R = O.euler_rotation(*W.cli_rotation(yaw=float(rng.uniform(0, 2 * np.pi))))
+        frames.append((len(meshes) - 1, w, h, True, O.viewport_transform(w, h, O.scene_extent([m["bbox_max"]])), R))
+    return meshes, frames
+
+
+def run_config3(torch, stream, device, args):
+    """Config 3 through the batched path (one CUDA-graph replay per pass over all frames)
+    and through the plain per-frame path (clear + draw_mesh + resolve per frame, one
+    context per viewport size), both timed with CUDA events on the same stream."""
+    import sloth_gpu as S
+    meshes, specs = config3_frames()
+    ctx = S.Context(device, stream=stream.cuda_stream)
+    dev = [S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"], m["idx"], m["bbox_max"]) for m in meshes]
+    frames = [{"w": w, "h": h, "image": im, "U": U, "draws": [(dev[mi], R)]} for mi, w, h, im, U, R in specs]
+    batch = S.Batch(ctx, frames)
+    batch.render()
+    shape, _ = batch.autotune(reps=2)
+    batch.render()
+    torch.cuda.synchronize()
+    steps = max(3, args.batched_steps)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        batch.render()
+    b.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = a.elapsed_time(b) / steps
+
+    plain = {}
+    def plain_pass():
+        for f in frames:
+            key = (f["w"], f["h"], f["image"])
+            c = plain.get(key)
+            if c is None:
+                c = plain[key] = S.Context(device, stream=stream.cuda_stream)
+                c.set_viewport(f["w"], f["h"], f["image"])
+            c.set_utransform(f["U"])
+            c.clear()
+            for m, R in f["draws"]:
+                c.draw_mesh(m, R)
+            c.device_buffers()
+    plain_pass()
+    torch.cuda.synchronize()
+    psteps = max(2, steps // 4)
+    a.record(stream)
+    for _ in range(psteps):
+        plain_pass()
+    b.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = a.elapsed_time(b) / psteps
+
+    # the batched frames equal the plain ones bit for bit (spot check)
+    checked = 0
+    for i in (0, 17, 255, 256, len(frames) - 1):
+        f = frames[i]
+        key = (f["w"], f["h"], f["image"])
+        c = plain[key]
+        c.set_utransform(f["U"])
+        c.clear()
+        for m, R in f["draws"]:
+            c.draw_mesh(m, R)
+        pc, pz, pw = c.read()
+        bc, bz, bw = batch.read(i)
+        assert np.array_equal(pc, bc) and np.array_equal(pz.view(np.uint32), bz.view(np.uint32)) \
+            and np.array_equal(pw, bw), f"batched frame {i} differs from the plain path"
+        checked += 1
+    nframes = len(frames)
+    out = {"workload": CONFIG3, "frames": nframes,
+           "triangles": int(sum(m["rgb"].shape[0] for m in [meshes[s[0]] for s in specs])),
+           "batched_frames_per_s": 1000.0 * nframes / batched_ms, "batched_ms_per_pass": batched_ms,
+           "plain_frames_per_s": 1000.0 * nframes / plain_ms, "plain_ms_per_pass": plain_ms,
+           "batched_over_plain": plain_ms / batched_ms, "tile_shape": S.tile_shapes()[shape],
+           "bitexact_frames_checked": checked, "graph": True}
+    for c in plain.values():
+        c.close()
+    batch.close()
+    ctx.close()
+    return out
 
 
 def main():
@@ -369,6 +477,8 @@ def main():
     ap.add_argument("--no-depth-cull", action="store_true",
                     help="rasterize every triangle (SLOTH_OPTION_DEPTH_CULL 0)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched config-3 leg")
+    ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)

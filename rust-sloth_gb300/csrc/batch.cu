@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(1024) batch_newline_kernel(BatchDev b, const i
     int32_t *tree = kShared ? stree : f.fb.nltree;
     if (kShared) {
         for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) stree[i] = -1;
-        __syncthreads();
+        block_sync();
     }
     const uint32_t lo = (uint32_t)blk.y, hi = min(d.mesh.ntri, lo + kBatchNewlineChunk);
     for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(1024) batch_newline_kernel(BatchDev b, const i
         nltree_update(tree, n, yr.z, yr.w, v, kShared);
     }
     if (kShared) {
-        __syncthreads();
+        block_sync();
         for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) {
             const int32_t v = stree[i];
             if (v >= 0 && *(volatile int32_t *)&f.fb.nltree[i] < v) atomicMax(&f.fb.nltree[i], v);
@@ -150,8 +150,12 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_fill_kernel(BatchDev b
     fill_small(r, gtri, vp, sp, b.bb.tile_cursor + f.tile_off, b.bb.entries, b.bb.capacity);
 }
 
-// Persistent raster: CTAs take (frame, tile) items from a device-side queue until it is
-// empty.  Empty tiles cost one counter read.
+// Raster over every frame's tiles in one launch: each CTA takes one (frame, tile) item
+// from a device-side queue (warp 0 pulls items until it gets a non-empty tile) and
+// rasterizes it; the hardware block scheduler keeps the SMs fed as CTAs finish.  A CTA
+// handles exactly one item: in a CTA that looped over several items, warps were seen to
+// run ahead into a further pass over the same tile (barrier phases out of step) and to
+// overwrite its finished keys, so the loop is left to the block scheduler.
 template <int TW, int TH>
 __global__ void __launch_bounds__(kRasterThreads) batch_raster_kernel(BatchDev b)
 {
@@ -161,29 +165,29 @@ __global__ void __launch_bounds__(kRasterThreads) batch_raster_kernel(BatchDev b
         if (blockIdx.x == 0 && threadIdx.x == 0) *b.overflow = 1;
         return;
     }
-    for (;;) {
-        if (threadIdx.x == 0) {
-            uint32_t it;
-            do {
-                it = atomicAdd(b.queue_head, 1u);
-            } while (it < b.total_tiles && b.bb.tile_count[it] == 0);
-            s_item = it;
+    if (threadIdx.x < 32) {
+        uint32_t it = 0;
+        for (;;) {
+            if (threadIdx.x == 0) it = atomicAdd(b.queue_head, 1u);
+            it = __shfl_sync(0xffffffffu, it, 0);
+            if (it >= b.total_tiles || b.bb.tile_count[it] != 0) break;
         }
-        __syncthreads();
-        const uint32_t item = s_item;
-        __syncthreads();
-        if (item >= b.total_tiles) break;
-        // frame of the global tile: last frame whose first tile is <= item
-        uint32_t lo = 0, hi = b.nframes;
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (b.frame_tile_off[mid] <= item) lo = mid;
-            else hi = mid;
-        }
-        const BatchFrame &f = b.frames[lo];
-        raster_tile<TW, TH>(S, f.g, f.fb, (int)(item - f.tile_off), b.bb.tile_count[item],
-                            b.bb.entries + b.bb.tile_offset[item], b.depth_cull);
+        if (threadIdx.x == 0) s_item = it;
+        __syncwarp();
     }
+    block_sync();
+    const uint32_t item = s_item;
+    if (item >= b.total_tiles) return;
+    // frame of the global tile: last frame whose first tile is <= item
+    uint32_t lo = 0, hi = b.nframes;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (b.frame_tile_off[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    const BatchFrame &f = b.frames[lo];
+    raster_tile<TW, TH>(S, f.g, f.fb, (int)(item - f.tile_off), b.bb.tile_count[item],
+                        b.bb.entries + b.bb.tile_offset[item], b.depth_cull);
 }
 
 // blocks[i] = (frame, first cell).
@@ -244,9 +248,8 @@ cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nb
 cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, cudaStream_t s)
 {
     if (!b.total_tiles) return cudaSuccess;
-    // persistent: as many CTAs as fit on the GPU (152 SMs x 4 resident CTAs), never more
-    // than there are tiles
-    const uint32_t grid = b.total_tiles < 152u * 4u ? b.total_tiles : 152u * 4u;
+    // one CTA per queue item (a CTA whose pulls only find empty tiles exits at once)
+    const uint32_t grid = b.total_tiles;
 #define SLOTH_BATCH_RASTER_CASE(W_, H_)                                                        \
     if (tw == W_ && th == H_) {                                                                \
         batch_raster_kernel<W_, H_><<<grid, kRasterThreads, 0, s>>>(b);                        \

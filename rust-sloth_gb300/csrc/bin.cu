@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
         if (lane >= d) v += o;
     }
     if (lane == 31) warp_sums[wid] = v;
-    __syncthreads();
+    block_sync();
     if (wid == 0) {
         uint32_t s = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0u;
 #pragma unroll
@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
         }
         warp_sums[lane] = s;
     }
-    __syncthreads();
+    block_sync();
     uint32_t run = v - local + (wid > 0 ? warp_sums[wid - 1] : 0u);   // exclusive prefix
     for (uint32_t i = lo; i < hi; ++i) {
         bb.tile_offset[i] = run;

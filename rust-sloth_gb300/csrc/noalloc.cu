@@ -69,7 +69,7 @@ noalloc_raster_kernel(uint32_t ntri, FrameGeom g, FrameBuffers fb)
     const int R0 = tr * TH, C0 = tc * TW;
     for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) skeys[i] = kEmptyKey;
     if (threadIdx.x == 0) s_next = 0;
-    __syncthreads();
+    block_sync();
     const int lane = threadIdx.x & 31;
     const Viewport vp{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
     uint32_t frags = 0;
@@ -109,7 +109,7 @@ noalloc_raster_kernel(uint32_t ntri, FrameGeom g, FrameBuffers fb)
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) frags += __shfl_xor_sync(0xffffffffu, frags, d);
     if (lane == 0) s_frags[threadIdx.x >> 5] = frags;
-    __syncthreads();
+    block_sync();
     unsigned long long *gk = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)R0 * g.pitch + C0;
     for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
         const int rr = i / TW, cc = i - rr * TW;

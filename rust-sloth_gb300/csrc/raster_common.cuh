@@ -131,7 +131,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         while (np2 < n) np2 <<= 1;
         for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) S.ent[i] = i < n ? entries[base + i] : ~0ull;
         if (threadIdx.x == 0) S.next = 0;
-        __syncthreads();
+        block_sync();
         if (depth_cull) {
             // bitonic sort, ascending: front-to-back depth bounds
             for (uint32_t k = 2; k <= np2; k <<= 1)
@@ -146,7 +146,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                             }
                         }
                     }
-                    __syncthreads();
+                    block_sync();
                 }
         }
         for (;;) {
@@ -182,24 +182,30 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
             if (!W.empty())
                 raster_part<TW, 0>(r, gtri, clip_wrapped(vp, W, tr, tc), R0, C0, g.w, S.keys, lane, frags);
         }
-        __syncthreads();
+        block_sync();
     }
     // fragment count: warp reduce, then one atomic per tile
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) frags += __shfl_xor_sync(0xffffffffu, frags, d);
     if (lane == 0) S.frags[threadIdx.x >> 5] = frags;
-    __syncthreads();
+    __syncwarp();
+    block_sync();
     for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
         const int rr = i / TW, cc = i - rr * TW;
         gk[(size_t)rr * g.pitch + cc] = S.keys[i];
     }
-    if (threadIdx.x == 0) {
-        uint32_t tot = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) tot += S.frags[k];
-        atomicAdd(fb.fragments, (unsigned long long)tot);
-        fb.tile_gen[tile] = fb.gen;
+    if (threadIdx.x < 32) {
+        // warp 0, converged: sum the per-warp counts, one atomic, tile generation
+        uint32_t tot = lane < (int)(blockDim.x >> 5) ? S.frags[lane] : 0u;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, d);
+        if (lane == 0) {
+            atomicAdd(fb.fragments, (unsigned long long)tot);
+            fb.tile_gen[tile] = fb.gen;
+        }
+        __syncwarp();
     }
-    __syncthreads();
+    block_sync();
 }
 
 }  // namespace sloth

@@ -101,7 +101,7 @@ newline_kernel(uint32_t ntri, uint32_t tri_base, uint32_t chunk, FrameGeom g, Fr
     int32_t *tree = kShared ? stree : fb.nltree;
     if (kShared) {
         for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) stree[i] = -1;
-        __syncthreads();
+        block_sync();
     }
     const uint32_t lo = blockIdx.x * chunk, hi = min(ntri, lo + chunk);
     for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
@@ -110,7 +110,7 @@ newline_kernel(uint32_t ntri, uint32_t tri_base, uint32_t chunk, FrameGeom g, Fr
         nltree_update(tree, n, yr.z, yr.w, v, kShared);
     }
     if (kShared) {
-        __syncthreads();
+        block_sync();
         for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) {
             const int32_t v = stree[i];
             if (v >= 0 && *(volatile int32_t *)&fb.nltree[i] < v) atomicMax(&fb.nltree[i], v);

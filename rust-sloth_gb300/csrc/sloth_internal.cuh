@@ -18,6 +18,17 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 
+// Block barrier.  __syncthreads compiles to an aligned barrier, which expects every warp
+// to arrive converged; after lane-dependent code (single-lane sections, loops whose trip
+// count differs between lanes) a warp is first reconverged with __syncwarp.  Without it a
+// warp can be counted before all its lanes arrive, and the barriers of the block fall out
+// of step.
+__device__ __forceinline__ void block_sync()
+{
+    __syncwarp();
+    __syncthreads();
+}
+
 constexpr float kFltMax = 3.40282347e+38f;
 constexpr uint64_t kEmptyKey = ~0ull;
 constexpr uint32_t kSmallMaxTilesDev = 8;   // triangles over more tiles are binned by warps

@@ -21,6 +21,7 @@ LIB_PATH = HERE / "_build" / "libsloth_gpu.so"
 
 OK = 0
 OPTION_DEPTH_CULL = 1
+OPTION_TILE_SHAPE = 2
 STATUS ={0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "LIMIT", 5: "DEVICE_FAULT"}
 
 # Every symbol declared in include/sloth_gpu.h, with (restype, argtypes).
@@ -58,6 +59,16 @@ SIGNATURES = {
     "sloth_ctx_set_option": (C.c_int, [_vp, C.c_int, C.c_int64]),
     "sloth_render_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_uint32, _vp, _f32p, C.c_uint32, C.c_uint32,
                                        C.c_int, _vp, _vp, _vp, _vp]),
+    "sloth_tile_shape": (C.c_int, [C.c_int, _u32p, _u32p]),
+    "sloth_batch_create": (C.c_int, [_vp, _vp, C.c_uint32, _vp, C.c_uint32, C.POINTER(_vp)]),
+    "sloth_batch_destroy": (None, [_vp]),
+    "sloth_batch_set_transforms": (C.c_int, [_vp, _f32p]),
+    "sloth_batch_render": (C.c_int, [_vp]),
+    "sloth_batch_read": (C.c_int, [_vp, C.c_uint32, _u32p, _f32p, _i32p]),
+    "sloth_batch_frame_buffers": (C.c_int, [_vp, C.c_uint32, C.POINTER(_vp), C.POINTER(_vp)]),
+    "sloth_batch_fragments": (C.c_int, [_vp, _u64p]),
+    "sloth_batch_set_tile_shape": (C.c_int, [_vp, C.c_int]),
+    "sloth_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "sloth_ctx_set_timing": (C.c_int, [_vp, C.c_int]),
     "sloth_ctx_kernel_time": (C.c_int, [_vp, C.c_char_p, C.POINTER(C.c_double), _u64p]),
     "sloth_ctx_launch_count": (C.c_uint64, [_vp]),
@@ -211,6 +222,10 @@ class Context:
         self._check(self.lib.sloth_ctx_fragments(self.h, C.byref(f)))
         return f.value
 
+    def set_tile_shape(self, shape: int):
+        """SLOTH_OPTION_TILE_SHAPE (index into tile_shapes()); applies at the next clear."""
+        self._check(self.lib.sloth_ctx_set_option(self.h, OPTION_TILE_SHAPE, shape))
+
     def set_depth_cull(self, on: bool):
         """SLOTH_OPTION_DEPTH_CULL: skip triangles proven hidden (same results)."""
         self._check(self.lib.sloth_ctx_set_option(self.h, OPTION_DEPTH_CULL, 1 if on else 0))
@@ -272,6 +287,96 @@ class Mesh:
             self.close()
         except Exception:
             pass
+
+
+class FrameDesc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("image", C.c_int32),
+                ("utransform", C.c_float * 16), ("first_draw", C.c_uint32), ("ndraws", C.c_uint32)]
+
+
+class DrawDesc(C.Structure):
+    _fields_ = [("mesh", C.c_void_p), ("transform", C.c_float * 16)]
+
+
+def tile_shapes() -> list[tuple[int, int]]:
+    lib = load_library()
+    out, i = [], 0
+    w, h = C.c_uint32(), C.c_uint32()
+    while lib.sloth_tile_shape(i, C.byref(w), C.byref(h)) == OK:
+        out.append((w.value, h.value))
+        i += 1
+    return out
+
+
+class Batch:
+    """Many frames rendered together (sloth_batch_*).
+
+    frames: list of dicts {w, h, image, U, draws: [(Mesh, R), ...]}; each frame is drawn
+    like ctx.clear() + ctx.draw_mesh(mesh, R) for its draws in order."""
+
+    def __init__(self, ctx: Context, frames):
+        self.ctx, self.lib = ctx, ctx.lib
+        draws = [d for f in frames for d in f["draws"]]
+        self._meshes = [m for m, _ in draws]   # keep alive
+        fa = (FrameDesc * len(frames))()
+        first = 0
+        self.sizes = []
+        for i, f in enumerate(frames):
+            fa[i].width, fa[i].height, fa[i].image = f["w"], f["h"], 1 if f["image"] else 0
+            for k, v in enumerate(_mat(f["U"])):
+                fa[i].utransform[k] = float(v)
+            fa[i].first_draw, fa[i].ndraws = first, len(f["draws"])
+            first += len(f["draws"])
+            nz = f["w"] * f["h"]
+            self.sizes.append((nz + (f["h"] if f["image"] else 0), nz))
+        da = (DrawDesc * max(1, len(draws)))()
+        for i, (m, R) in enumerate(draws):
+            da[i].mesh = m.h
+            for k, v in enumerate(_mat(R)):
+                da[i].transform[k] = float(v)
+        h = C.c_void_p()
+        ctx._check(self.lib.sloth_batch_create(ctx.h, C.cast(fa, C.c_void_p), len(frames), C.cast(da, C.c_void_p),
+                                               len(draws), C.byref(h)))
+        self.h = h
+        self.ndraws = len(draws)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sloth_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self):
+        self.ctx._check(self.lib.sloth_batch_render(self.h))
+
+    def set_transforms(self, mats):
+        a = np.ascontiguousarray(np.asarray(mats, np.float32).reshape(self.ndraws * 16))
+        self.ctx._check(self.lib.sloth_batch_set_transforms(self.h, _ptr(a, C.c_float)))
+
+    def read(self, frame: int):
+        nf, nz = self.sizes[frame]
+        c, z, w = np.empty(nf, np.uint32), np.empty(nz, np.float32), np.empty(nz, np.int32)
+        self.ctx._check(self.lib.sloth_batch_read(self.h, frame, _ptr(c, C.c_uint32), _ptr(z, C.c_float),
+                                                  _ptr(w, C.c_int32)))
+        return c, z, w
+
+    def fragments(self) -> int:
+        f = C.c_uint64()
+        self.ctx._check(self.lib.sloth_batch_fragments(self.h, C.byref(f)))
+        return f.value
+
+    def set_tile_shape(self, shape: int):
+        self.ctx._check(self.lib.sloth_batch_set_tile_shape(self.h, shape))
+
+    def autotune(self, reps: int = 3):
+        s, ms = C.c_int(), C.c_float()
+        self.ctx._check(self.lib.sloth_batch_autotune(self.h, reps, C.byref(s), C.byref(ms)))
+        return s.value, ms.value
 
 
 def cells_to_text(cells: np.ndarray) -> str:

@@ -1,0 +1,128 @@
+"""The batched path (sloth_batch_*): many frames of uneven meshes and viewports in one
+pass of each stage, one persistent raster pass and a CUDA graph.  Every frame must be
+bit-identical to the oracle drawing that frame alone; so must the single-frame path
+with every tile shape."""
+import math
+
+import numpy as np
+import pytest
+
+import sloth_gpu as S
+import workloads as W
+from oracle import oracle as O
+from gpu_helpers import assert_same, gpu_render, oracle_render
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = S.Context(0)
+    yield c
+    c.close()
+
+
+def dev_mesh(ctx, m):
+    return S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"], m.get("idx"), m.get("bbox_max"))
+
+
+def mixed_frames(ctx):
+    """Host meshes + a frame list mixing sizes, image modes, wraps and multi-draw frames."""
+    sphere = W.uv_sphere()
+    ico = W.displaced_icosphere(3, seed=3)
+    soup_a = W.soup(4000, seed=31, n_large=12)
+    soup_b = W.soup(1500, seed=32, n_large=4, sigma=0.06)
+    meshes = {"sphere": sphere, "ico": ico, "a": soup_a, "b": soup_b}
+    dev = {k: dev_mesh(ctx, m) for k, m in meshes.items()}
+    rng = np.random.default_rng(5)
+    frames = []
+    specs = [(160, 48, True, ["sphere"]), (640, 360, True, ["ico"]), (80, 24, False, ["a"]),
+             (161, 47, True, ["a", "b"]), (300, 200, True, ["b", "sphere"]), (64, 64, False, ["ico", "a"]),
+             (1, 1, True, ["a"]), (33, 9, True, ["b"])]
+    for i in range(20):
+        w, h, image, names = specs[i % len(specs)]
+        ang = W.cli_rotation(yaw=float(rng.uniform(0, 2 * math.pi)), pitch=float(rng.uniform(-0.5, 0.5)))
+        R = O.euler_rotation(*ang)
+        ext = 0.7 if i % 3 == 0 else O.scene_extent([meshes[n]["bbox_max"] for n in names])
+        U = O.viewport_transform(w, h, ext)
+        frames.append({"w": w, "h": h, "image": image, "U": U, "names": names, "R": R,
+                       "draws": [(dev[n], R) for n in names]})
+    return meshes, dev, frames
+
+
+def check_frames(batch, meshes, frames, label):
+    for i, f in enumerate(frames):
+        ref = oracle_render([meshes[n] for n in f["names"]], f["R"], f["w"], f["h"], f["image"], U=f["U"])
+        cells, z, winner = batch.read(i)
+        assert_same((cells, z, winner, None), ref, f"{label} frame {i} {f['w']}x{f['h']}")
+
+
+def test_batch_matches_oracle_and_replays(ctx):
+    meshes, dev, frames = mixed_frames(ctx)
+    b = S.Batch(ctx, frames)
+    b.render()                                   # planned render (sizes the entries)
+    check_frames(b, meshes, frames, "planned")
+    for k in range(3):                           # graph capture + replays
+        b.render()
+    check_frames(b, meshes, frames, "graph")
+    # new transforms for every draw, replayed through the same graph
+    rng = np.random.default_rng(9)
+    mats = []
+    for f in frames:
+        R = O.euler_rotation(*W.cli_rotation(yaw=float(rng.uniform(0, 6.28))))
+        f["R"] = R
+        mats += [R] * len(f["draws"])
+    b.set_transforms(np.stack(mats))
+    b.render()
+    check_frames(b, meshes, frames, "new transforms")
+    b.close()
+
+
+def test_batch_every_tile_shape_and_autotune(ctx):
+    meshes, dev, frames = mixed_frames(ctx)
+    frames = frames[:8]
+    b = S.Batch(ctx, frames)
+    for shape in range(len(S.tile_shapes())):
+        b.set_tile_shape(shape)
+        b.render()
+        check_frames(b, meshes, frames, f"shape {S.tile_shapes()[shape]}")
+    best, ms = b.autotune(reps=2)
+    assert 0 <= best < len(S.tile_shapes()) and ms > 0
+    b.render()
+    check_frames(b, meshes, frames, "autotuned")
+    b.close()
+
+
+def test_batch_entry_overflow_replans(ctx):
+    """Transforms that list far more tile entries than the first render sized: the
+    raster reports the overflow and the read re-plans and re-renders."""
+    m = W.soup(3000, seed=41, n_large=10)
+    dm = dev_mesh(ctx, m)
+    small = np.diag([0.05, 0.05, 0.05, 1.0]).astype(np.float32)
+    R0 = O.mat4_mul(O.euler_rotation(*W.cli_rotation()), small)
+    U = O.viewport_transform(640, 360, 1.0)
+    frames = [{"w": 640, "h": 360, "image": True, "U": U, "draws": [(dm, R0)]} for _ in range(3)]
+    b = S.Batch(ctx, frames)
+    b.render()
+    b.render()                      # graph captured with the small entry buffer
+    R1 = O.euler_rotation(*W.cli_rotation(yaw=0.3))
+    b.set_transforms(np.stack([R1] * 3))
+    b.render()                      # the graph overflows the entry buffer
+    ref = oracle_render([m], R1, 640, 360, True, U=U)
+    for i in range(3):
+        assert_same((*b.read(i), None), ref, f"overflow frame {i}")
+    b.close()
+
+
+@pytest.mark.parametrize("shape", range(5))
+def test_context_every_tile_shape(ctx, shape):
+    m = W.soup(6000, seed=51, n_large=15)
+    R = O.euler_rotation(*W.cli_rotation(yaw=0.9, pitch=0.3))
+    ctx.set_tile_shape(shape)
+    try:
+        for w, h, image in [(321, 181, True), (640, 360, False)]:
+            U = O.viewport_transform(w, h, 0.75)
+            ref = oracle_render([m], R, w, h, image, U=U)
+            assert_same(gpu_render(ctx, [m], R, w, h, image, U=U), ref, f"shape {shape} {w}x{h}")
+    finally:
+        ctx.set_tile_shape(0)
