@@ -220,7 +220,15 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # One dedicated stream for the library, the L2 flush and the timing events: the legacy
+    # default stream (handle 0) would make the library create its own non-blocking stream,
+    # which events recorded on stream 0 do not bracket.
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    if args.only_diff:
+        print(json.dumps({"differentiable": run_config4(torch, stream, local, args),
+                          "inverse_rendering": run_config5(torch, stream, local, args)}), flush=True)
+        return 0
     m = make_workload()
     ntri = int(m["rgb"].shape[0])
     R = S.euler_rotation(*W.cli_rotation())
@@ -340,6 +348,10 @@ def run_gpu(args):
     batched = None
     if not args.no_batched:
         batched = run_config3(torch, stream, local, args)
+    differentiable = inverse = None
+    if not args.no_diff:
+        differentiable = run_config4(torch, stream, local, args)
+        inverse = run_config5(torch, stream, local, args)
 
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
@@ -353,7 +365,7 @@ def run_gpu(args):
         "depth_cull": not args.no_depth_cull,
         "e2e": e2e,
         "gpu_launches": launches, "kernels": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
-        "batched": batched,
+        "batched": batched, "differentiable": differentiable, "inverse_rendering": inverse,
     }
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -465,6 +477,176 @@ def run_config3(torch, stream, device, args):
     return out
 
 
+CONFIG4 = ("config4: icosphere subdivision 5 (20,480 triangles), 32 views at 512x512 with yaw uniform in "
+           "[0, 2pi), f32 vertex colours U[0,1], light (0.577, 0.577, 0.577); loss = sum of squared "
+           "differences to targets rendered from vertices perturbed by N(0, 0.01)")
+
+
+def _views(rng, n, w, h, ext, pitch_range=0.0):
+    from oracle import oracle as O
+    import workloads as W
+    U = O.viewport_transform(w, h, ext)
+    out = []
+    for _ in range(n):
+        yaw = float(rng.uniform(0.0, 2.0 * np.pi))
+        pitch = float(rng.uniform(-pitch_range, pitch_range)) if pitch_range else 0.0
+        out.append({"w": w, "h": h, "image": False, "U": U,
+                    "R": O.euler_rotation(*W.cli_rotation(yaw=yaw, pitch=pitch))})
+    return out
+
+
+def _event_ms(torch, stream, fn, reps):
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def run_config4(torch, stream, device, args):
+    """Forward (render + shade) and backward (adjoint) of config 4 with stored and with
+    recomputed visibility; gradients checked against the f64 CPU adjoint on interior
+    cells (samples >= 1 px inside their triangle)."""
+    import diff_render as DR
+    import sloth_gpu as S
+    import workloads as W
+    from oracle import diff_shade as D
+    from oracle import oracle as O
+    rng = np.random.default_rng(44)
+    m = W.displaced_icosphere(5, seed=4, amplitude=0.0)
+    nv = m["x"].size
+    views = _views(rng, 32, 512, 512, O.scene_extent([m["bbox_max"]]))
+    dev = torch.device("cuda", device)
+    light = torch.tensor([0.577, 0.577, 0.577], dtype=torch.float32, device=dev)
+    vrgb = torch.from_numpy(rng.uniform(0, 1, (nv, 3)).astype(np.float32)).to(dev)
+    pos0 = np.stack([m["x"], m["y"], m["z"]], 1).astype(np.float32)
+    pos = torch.from_numpy(pos0).to(dev)
+    tpos = torch.from_numpy(pos0 + rng.normal(0, 0.01, pos0.shape).astype(np.float32)).to(dev)
+    ctx = S.Context(device, stream=stream.cuda_stream)
+    out = {"workload": CONFIG4, "views": len(views), "triangles": int(m["rgb"].shape[0])}
+    reps = max(3, args.batched_steps)
+    for store in (True, False):
+        sv = DR.ShadedViews(ctx, m, views, stream, store_visibility=store)
+        sv.render(tpos)
+        target = sv.shade(vrgb, light)
+        sv.render(pos)
+        rgb = sv.shade(vrgb, light)
+        grad = (2.0 * (rgb - target)).contiguous()
+
+        def fwd():
+            sv.render(pos)
+            sv.shade(vrgb, light)
+
+        def bwd():
+            sv.shade_backward(vrgb, light, grad)
+
+        for _ in range(3):
+            fwd()
+            bwd()
+        f_ms = _event_ms(torch, stream, fwd, reps)
+        fwd()
+        b_ms = _event_ms(torch, stream, bwd, reps)
+        key = "stored" if store else "recomputed"
+        out[key] = {"forward_ms_per_pass": f_ms, "backward_ms_per_pass": b_ms,
+                    "forward_ms_per_frame": f_ms / len(views), "backward_ms_per_frame": b_ms / len(views),
+                    "backward_over_forward": b_ms / f_ms,
+                    "visibility_bytes": sv.ncells * DR.ShadedViews.VIS_BYTES_PER_CELL if store else 0}
+        if store:
+            # the adjoint of the loss restricted to interior cells vs the f64 CPU adjoint
+            fwd()
+            torch.cuda.synchronize()
+            g_h = grad.cpu().numpy().astype(np.float64)
+            masks, ovs = [], []
+            for i, v in enumerate(views):
+                f = O.render([m], v["R"], v["w"], v["h"], False, U=v["U"])
+                ov = D.View(O.mat4_mul(v["U"], v["R"]), f.winner, f.winner_xy)
+                ovs.append(ov)
+                masks.append(D.interior_cells(pos0.astype(np.float64), m["idx"], ov))
+            mask = np.concatenate(masks)
+            g_h[~mask] = 0.0
+            gm = torch.from_numpy(g_h.astype(np.float32)).to(dev)
+            gp, gc, gl = sv.shade_backward(vrgb, light, gm)
+            torch.cuda.synchronize()
+            rp, rc, rl = np.zeros((nv, 3)), np.zeros((nv, 3)), np.zeros(3)
+            vr = vrgb.cpu().numpy().astype(np.float64)
+            for i, ov in enumerate(ovs):
+                a, n = sv.cells[i]
+                p_, c_, l_ = D.shade_vjp(pos0.astype(np.float64), vr, np.array([0.577, 0.577, 0.577]), m["idx"], ov,
+                                         g_h[a:a + n])
+                rp += p_
+                rc += c_
+                rl += l_
+            rel = lambda x, r: float(np.linalg.norm(x.cpu().numpy().astype(np.float64) - r) / max(np.linalg.norm(r), 1e-30))
+            out["grad_check_vs_f64"] = {"interior_cells": int(mask.sum()), "pos_rel": rel(gp, rp),
+                                        "vertex_rgb_rel": rel(gc, rc), "light_rel": rel(gl, rl)}
+        sv.close()
+    torch.cuda.synchronize()
+    ctx.close()
+    return out
+
+
+CONFIG5 = ("config5: fit vertex colours and positions of an icosphere subdivision 4 (5,120 triangles, initial "
+           "colours 0.5) to 64 views at 256x256 of a displaced icosphere subdivision 6 (noise amplitude 0.1, "
+           "value-noise vertex colours), 200 Adam steps (lr 1e-2), light (0.577, 0.577, 0.577)")
+
+
+def run_config5(torch, stream, device, args, steps=200):
+    """Inverse rendering: Adam on vertex positions and colours through the differentiable
+    path, visibility stored (it fits the 1 GB budget) and recomputed."""
+    import diff_render as DR
+    import sloth_gpu as S
+    import workloads as W
+    from oracle import oracle as O
+    rng = np.random.default_rng(55)
+    tgt = W.displaced_icosphere(6, seed=6, amplitude=0.1)
+    tcol = W.vertex_colours(tgt, seed=60)
+    fit = W.displaced_icosphere(4, seed=0, amplitude=0.0)
+    views = _views(rng, 64, 256, 256, O.scene_extent([tgt["bbox_max"]]), pitch_range=0.6)
+    dev = torch.device("cuda", device)
+    light = torch.tensor([0.577, 0.577, 0.577], dtype=torch.float32, device=dev)
+    ctx = S.Context(device, stream=stream.cuda_stream)
+    sv_t = DR.ShadedViews(ctx, tgt, views, stream)
+    tp = torch.from_numpy(np.stack([tgt["x"], tgt["y"], tgt["z"]], 1).astype(np.float32)).to(dev)
+    target = DR.shade_views(tp, torch.from_numpy(tcol).to(dev), light, sv_t).detach().clone()
+    sv_t.close()
+    out = {"workload": CONFIG5, "views": len(views), "steps": steps}
+    p0 = np.stack([fit["x"], fit["y"], fit["z"]], 1).astype(np.float32)
+    for store in (None, False):
+        sv = DR.ShadedViews(ctx, fit, views, stream, store_visibility=store, vis_budget_bytes=1 << 30)
+        pos = torch.from_numpy(p0).to(dev).requires_grad_(True)
+        col = torch.full((p0.shape[0], 3), 0.5, dtype=torch.float32, device=dev, requires_grad=True)
+        opt = torch.optim.Adam([pos, col], lr=1e-2)
+
+        def rmse():
+            with torch.no_grad():
+                return float(torch.sqrt(((DR.shade_views(pos, col, light, sv) - target) ** 2).mean()))
+
+        r0 = rmse()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        a.record(stream)
+        for _ in range(steps):
+            opt.zero_grad(set_to_none=True)
+            loss = ((DR.shade_views(pos, col, light, sv) - target) ** 2).sum()
+            loss.backward()
+            opt.step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        key = "stored" if sv.store_visibility else "recomputed"
+        out[key] = {"steps_per_s": steps / wall, "device_ms_per_step": a.elapsed_time(b) / steps,
+                    "rmse_initial": r0, "rmse_final": rmse(),
+                    "visibility_bytes": sv.ncells * DR.ShadedViews.VIS_BYTES_PER_CELL if sv.store_visibility else 0}
+        sv.close()
+    torch.cuda.synchronize()
+    ctx.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -479,6 +661,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched config-3 leg")
     ap.add_argument("--batched-steps", type=int, default=20)
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiable legs (configs 4 and 5)")
+    ap.add_argument("--only-diff", action="store_true", help="run only the differentiable legs (configs 4 and 5)")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)

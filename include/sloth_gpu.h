@@ -154,7 +154,8 @@ void sloth_mesh_destroy(sloth_mesh *mesh);
 
 /* Overwrite a mesh's vertex positions and face colours in place (same nvert/ntri), with
  * asynchronous copies on the context's stream; page-locked host buffers make them true
- * async copies.  The buffers must stay valid until the next synchronising call. */
+ * async copies.  The sources may be host or device memory (unified addressing decides
+ * the copy direction).  The buffers must stay valid until the next synchronising call. */
 sloth_status sloth_mesh_update(sloth_mesh *mesh, const float *x, const float *y, const float *z,
                                const uint8_t *rgb);
 sloth_status sloth_mesh_info(const sloth_mesh *mesh, uint32_t *ntri, float bbox_max[3]);
@@ -214,6 +215,42 @@ sloth_status sloth_batch_set_tile_shape(sloth_batch *batch, int shape);
 /* Autotuner: render the batch `reps` times with every tile shape, keep the fastest;
  * reports the shape and its mean render time in ms. */
 sloth_status sloth_batch_autotune(sloth_batch *batch, int reps, int *best_shape, float *best_ms);
+
+/* ---- differentiable shading of a rendered batch ----------------------------------- */
+
+/* No counterpart in the reference, which only maps the screen-space normal's z to a
+ * character (src/rasterizer.rs:76, default_shader at src/rasterizer.rs:5-27).  These
+ * calls define a smooth f32 image on the visibility of the last render and its adjoint,
+ * for fitting a mesh to images (inverse rendering).
+ *
+ * Every draw of the batch must use one mesh.  For the winning sample (x, y) of depth
+ * cell c of a frame (the triangle whose depth key won the cell, as in the render), with
+ * A, B, C that triangle's vertices after the draw's utransform*transform:
+ *     rgb[c] = (b0*col(A) + b1*col(B) + b2*col(C)) * clamp(n . L, 0, 1)
+ * b_i the barycentric weights of (x, y) in the 2-D triangle (ABC), n the unit normal of
+ * (B-A) x (C-A), col the per-vertex colour (vertex_rgb, 3 floats per mesh vertex) and L
+ * the light direction in screen space (L = (0,0,1) makes the shade factor the
+ * reference's normal z).  Cells without a winner, and zero-area triangles, give 0.
+ * Visibility (which triangle and sample) is piecewise constant in the vertex positions
+ * and is not differentiated.
+ *
+ * rgb holds 3 floats per depth cell of every frame, frames in order
+ * (sloth_batch_depth_cells gives a frame's offset and size, in cells).  vertex_rgb, light
+ * (3 floats), rgb and every gradient buffer are device memory; calls are asynchronous on
+ * the context's stream.  With store_visibility = 1 the forward call also keeps the
+ * winning (triangle, sample) of every cell (8 bytes per depth cell) for the next backward
+ * call; otherwise the backward call decodes it again from the depth keys.  Either way the
+ * backward call must follow the render it differentiates, before the next render. */
+sloth_status sloth_batch_depth_cells(sloth_batch *batch, uint32_t frame, uint64_t *first, uint64_t *count);
+sloth_status sloth_batch_shade(sloth_batch *batch, const float *vertex_rgb, const float *light, float *rgb,
+                               int store_visibility);
+/* Adds d(loss)/d(vertex position) (3 floats per mesh vertex, object space, i.e. the x, y,
+ * z arrays of sloth_mesh_create/update), d(loss)/d(vertex_rgb) and d(loss)/d(light) to
+ * grad_pos, grad_vertex_rgb and grad_light (any may be NULL), for grad_rgb =
+ * d(loss)/d(rgb).  The sums use float atomics, so their last bits vary run to run. */
+sloth_status sloth_batch_shade_backward(sloth_batch *batch, const float *vertex_rgb, const float *light,
+                                        const float *grad_rgb, float *grad_pos, float *grad_vertex_rgb,
+                                        float *grad_light);
 
 /* ---- one frame without device allocation ------------------------------------------ */
 

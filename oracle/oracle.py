@@ -22,6 +22,7 @@ class OrcCtx(C.Structure):
         ("z", C.POINTER(C.c_float)), ("cells", C.POINTER(C.c_uint32)),
         ("winner", C.POINTER(C.c_int32)),
         ("fragments", C.c_uint64), ("candidates", C.c_uint64), ("next_tri", C.c_uint32),
+        ("winner_xy", C.POINTER(C.c_uint32)),
     ]
 
 
@@ -128,6 +129,7 @@ class Frame:
     winner: np.ndarray    # int32 per depth cell
     fragments: int
     candidates: int
+    winner_xy: np.ndarray = None   # uint32 per depth cell: sample x | y << 16 (0xffffffff: none)
 
 
 class Oracle:
@@ -139,6 +141,7 @@ class Oracle:
         self.z = np.empty(n, np.float32)
         self.cells = np.empty(n + (height if image else 0), np.uint32)
         self.winner = np.empty(n, np.int32)
+        self.winner_xy = np.empty(n, np.uint32)
         self.c = OrcCtx()
         self.c.width, self.c.height, self.c.image = width, height, 1 if image else 0
         for i, v in enumerate(_m(U)):
@@ -146,6 +149,7 @@ class Oracle:
         self.c.z = _p(self.z, C.c_float)
         self.c.cells = _p(self.cells, C.c_uint32)
         self.c.winner = _p(self.winner, C.c_int32)
+        self.c.winner_xy = _p(self.winner_xy, C.c_uint32)
         self.clear()
 
     def clear(self):
@@ -174,7 +178,7 @@ class Oracle:
 
     def frame(self) -> Frame:
         return Frame(self.cells.copy(), self.z.copy(), self.winner.copy(),
-                     int(self.c.fragments), int(self.c.candidates))
+                     int(self.c.fragments), int(self.c.candidates), self.winner_xy.copy())
 
 
 def render(meshes, R, width, height, image, U=None, threads: int = 1) -> Frame:

@@ -55,6 +55,8 @@ void orc_clear(orc_ctx *ctx)
     for (uint64_t i = 0; i < n; ++i) ctx->z[i] = ORC_FLT_MAX;
     if (ctx->winner)
         for (uint64_t i = 0; i < n; ++i) ctx->winner[i] = -1;
+    if (ctx->winner_xy)
+        for (uint64_t i = 0; i < n; ++i) ctx->winner_xy[i] = 0xffffffffu;
     ctx->fragments = 0;
     ctx->candidates = 0;
     ctx->next_tri = 0;
@@ -225,7 +227,8 @@ static void triangle_setup(const orc_ctx *ctx, const float v[9], const uint8_t r
 
 /* The body of one sample, src/rasterizer.rs:71-86.  Returns 1 if covered. */
 static inline int sample(orc_ctx *ctx, const orc_setup *s, uint64_t x, uint64_t y,
-                         float *zcell, uint32_t *fb_id, uint32_t *fb_id1, int32_t *win)
+                         float *zcell, uint32_t *fb_id, uint32_t *fb_id1, int32_t *win,
+                         uint32_t *wxy)
 {
     const float (*v)[3] = s->v;
     float px = (float)x, py = (float)y;
@@ -241,6 +244,7 @@ static inline int sample(orc_ctx *ctx, const orc_setup *s, uint64_t x, uint64_t 
             if (fb_id) *fb_id = px_cell;
             if (fb_id1) *fb_id1 = px_cell;
             if (win) *win = (int32_t)s->tri;
+            if (wxy) *wxy = (uint32_t)x | ((uint32_t)y << 16);
         }
         (void)ctx;
         return 1;
@@ -260,7 +264,8 @@ void orc_draw_triangle(orc_ctx *ctx, const float v[9], const uint8_t rgb[3], con
             ctx->candidates++;
             ctx->fragments += (uint64_t)sample(ctx, &s, x, y, &ctx->z[id], &ctx->cells[id],
                                                &ctx->cells[id + 1],
-                                               ctx->winner ? &ctx->winner[id] : NULL);
+                                               ctx->winner ? &ctx->winner[id] : NULL,
+                                               ctx->winner_xy ? &ctx->winner_xy[id] : NULL);
         }
         if (ctx->image) ctx->cells[y * w + 1] = ORC_CELL('\n', 0, 0, 0);
     }
@@ -328,11 +333,12 @@ static void run_band(band_job *j)
                     j->candidates++;
                     j->fragments += (uint64_t)sample(ctx, s, x, y, &ctx->z[id], &ctx->cells[id],
                                                      id + 1 < hi ? &ctx->cells[id + 1] : NULL,
-                                                     ctx->winner ? &ctx->winner[id] : NULL);
+                                                     ctx->winner ? &ctx->winner[id] : NULL,
+                                                     ctx->winner_xy ? &ctx->winner_xy[id] : NULL);
                 } else if (j->ra > 0 && id == ghost) {
                     /* the depth test of the cell above the band decides the write of
                        this band's first frame cell (its id+1 write) */
-                    sample(ctx, s, x, y, &j->ghost_z, NULL, &ctx->cells[lo], NULL);
+                    sample(ctx, s, x, y, &j->ghost_z, NULL, &ctx->cells[lo], NULL, NULL);
                 }
             }
             if (ctx->image) {

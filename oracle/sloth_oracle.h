@@ -42,6 +42,8 @@ typedef struct {
     uint64_t fragments;     /* covered samples (all three edge functions >= 0) */
     uint64_t candidates;    /* samples visited by the loops */
     uint32_t next_tri;      /* global triangle counter since clear (draw order) */
+    uint32_t *winner_xy;    /* optional (may be NULL): w*h, sample point x | y << 16 of the
+                               last accepted depth write (differentiable shading's visibility) */
 } orc_ctx;
 
 /* src/rasterizer.rs:5-27 default_shader: shade -> ASCII ramp char. */

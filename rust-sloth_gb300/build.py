@@ -19,7 +19,7 @@ OUT_DIR = HERE / "_build"
 LIB = OUT_DIR / "libsloth_gpu.so"
 
 SOURCES = ["setup.cu", "bin.cu", "raster.cu", "resolve.cu", "sloth_api.cu", "noalloc.cu", "batch.cu",
-           "batch_api.cu"]
+           "batch_api.cu", "diff.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-ftz=false",

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "batch_kernels.h"
+#include "diff_kernels.h"
 #include "sloth_gpu.h"
 #include "sloth_internal.cuh"
 
@@ -61,6 +62,12 @@ struct sloth_batch {
 
     cudaGraphExec_t graph = nullptr;
     bool rendered = false;
+
+    // differentiable shading
+    int2 *diff_blk = nullptr;                 // (frame, first depth cell) per kDiffChunk
+    uint32_t ndiff_blk = 0;
+    uint2 *vis = nullptr;                     // stored visibility, one per depth cell
+    bool vis_valid = false;                   // vis holds the last render's visibility
 };
 
 // Shared with sloth_api.cu.
@@ -149,6 +156,7 @@ void set_mats(sloth_batch *b)
 sloth_status build(sloth_batch *b, int shape)
 {
     free_layout(b);
+    b->vis_valid = false;
     b->shape = shape;
     const int tw = kTileShapes[shape][0], th = kTileShapes[shape][1];
     const uint32_t nf = (uint32_t)b->frames.size(), nd = (uint32_t)b->meshes.size();
@@ -180,6 +188,9 @@ sloth_status build(sloth_batch *b, int shape)
         bf.g = g;
         bf.tile_off = tiles;
         bf.rec_off = (uint32_t)rec;
+        bf.first_draw = fd.first_draw;
+        bf.ndraws = fd.ndraws;
+        bf.z_off = zs;
         tile_off[f] = tiles;
         key_off[f] = keys;
         nl_off[f] = nl;
@@ -379,6 +390,31 @@ sloth_status settle(sloth_batch *b)
     return SLOTH_OK;
 }
 
+// Checks shared by the forward and backward shading calls; builds the block table.
+sloth_status diff_prepare(sloth_batch *b, const float *vertex_rgb, const float *light)
+{
+    if (!vertex_rgb || !light) return sloth_ctx_fail(b->ctx, SLOTH_ERR_INVALID_ARGUMENT, "vertex_rgb/light are NULL");
+    if (!b->rendered) return sloth_ctx_fail(b->ctx, SLOTH_ERR_INVALID_ARGUMENT, "render the batch first");
+    for (const sloth_mesh *m : b->meshes)
+        if (m != b->meshes[0])
+            return sloth_ctx_fail(b->ctx, SLOTH_ERR_INVALID_ARGUMENT, "shading needs one mesh for every draw");
+    BCU(b, cudaSetDevice(b->device));
+    if (!b->diff_blk) {
+        std::vector<int2> t;
+        for (uint32_t f = 0; f < (uint32_t)b->frames.size(); ++f) {
+            const uint64_t nz = b->z_off[f + 1] - b->z_off[f];
+            for (uint64_t c = 0; c < nz; c += kDiffChunk) t.push_back(make_int2((int)f, (int)c));
+        }
+        BCU(b, balloc(&b->diff_blk, t.size()));
+        if (!t.empty())
+            BCU(b, cudaMemcpy(b->diff_blk, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice));
+        b->ndiff_blk = (uint32_t)t.size();
+    }
+    // the keys of the last render must be complete (re-render if its entries overflowed)
+    return settle(b);
+}
+
+
 }  // namespace
 
 extern "C" {
@@ -437,6 +473,8 @@ void sloth_batch_destroy(sloth_batch *b)
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);
     free_layout(b);
+    bfree(b->diff_blk);
+    bfree(b->vis);
     if (b->h_mats) cudaFreeHost(b->h_mats);
     if (b->h_total) cudaFreeHost(b->h_total);
     if (b->h_overflow) cudaFreeHost(b->h_overflow);
@@ -457,6 +495,7 @@ sloth_status sloth_batch_render(sloth_batch *b)
 {
     if (!b) return SLOTH_ERR_INVALID_ARGUMENT;
     BCU(b, cudaSetDevice(b->device));
+    b->vis_valid = false;
     if (!b->rendered || !b->bb.entries) return render_planned(b);
     if (!b->graph && b->stream != nullptr) {
         const sloth_status st = capture(b);
@@ -553,6 +592,42 @@ sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, flo
     if (st != SLOTH_OK) return st;
     if (best_shape) *best_shape = best;
     if (best_ms) *best_ms = best_t;
+    return SLOTH_OK;
+}
+
+// ---- differentiable shading -------------------------------------------------------
+
+sloth_status sloth_batch_depth_cells(sloth_batch *b, uint32_t frame, uint64_t *first, uint64_t *count)
+{
+    if (!b || frame >= b->frames.size()) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (first) *first = b->z_off[frame];
+    if (count) *count = b->z_off[frame + 1] - b->z_off[frame];
+    return SLOTH_OK;
+}
+
+sloth_status sloth_batch_shade(sloth_batch *b, const float *vertex_rgb, const float *light, float *rgb,
+                               int store_visibility)
+{
+    if (!b || !rgb) return SLOTH_ERR_INVALID_ARGUMENT;
+    sloth_status st = diff_prepare(b, vertex_rgb, light);
+    if (st != SLOTH_OK) return st;
+    if (store_visibility && !b->vis) BCU(b, balloc(&b->vis, b->total_z));
+    BCU(b, launch_batch_shade(dev_view(b), b->diff_blk, b->ndiff_blk, vertex_rgb, light, rgb,
+                              store_visibility ? b->vis : nullptr, b->stream));
+    b->vis_valid = store_visibility != 0;
+    return SLOTH_OK;
+}
+
+sloth_status sloth_batch_shade_backward(sloth_batch *b, const float *vertex_rgb, const float *light,
+                                        const float *grad_rgb, float *grad_pos, float *grad_vertex_rgb,
+                                        float *grad_light)
+{
+    if (!b || !grad_rgb) return SLOTH_ERR_INVALID_ARGUMENT;
+    sloth_status st = diff_prepare(b, vertex_rgb, light);
+    if (st != SLOTH_OK) return st;
+    BCU(b, launch_batch_shade_backward(dev_view(b), b->diff_blk, b->ndiff_blk, vertex_rgb, light, grad_rgb,
+                                       b->vis_valid ? b->vis : nullptr, grad_pos, grad_vertex_rgb, grad_light,
+                                       b->stream));
     return SLOTH_OK;
 }
 

@@ -19,6 +19,9 @@ struct BatchFrame {
     FrameBuffers fb;           // pointers into the batch's buffers, records offset to the frame
     uint32_t tile_off;         // first global tile of the frame
     uint32_t rec_off;          // first global record of the frame
+    uint32_t first_draw;       // the frame's first draw
+    uint32_t ndraws;
+    uint64_t z_off;            // first depth cell of the frame in the batch's depth-cell order
 };
 
 struct BatchDraw {

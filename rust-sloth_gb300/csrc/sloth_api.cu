@@ -581,11 +581,11 @@ sloth_status sloth_mesh_update(sloth_mesh *m, const float *x, const float *y, co
     CU(ctx, cudaSetDevice(m->device));
     const size_t nb = (size_t)m->nvert * sizeof(float);
     if (m->nvert) {
-        CU(ctx, cudaMemcpyAsync(m->x, x, nb, cudaMemcpyHostToDevice, ctx->stream));
-        CU(ctx, cudaMemcpyAsync(m->y, y, nb, cudaMemcpyHostToDevice, ctx->stream));
-        CU(ctx, cudaMemcpyAsync(m->z, z, nb, cudaMemcpyHostToDevice, ctx->stream));
+        CU(ctx, cudaMemcpyAsync(m->x, x, nb, cudaMemcpyDefault, ctx->stream));
+        CU(ctx, cudaMemcpyAsync(m->y, y, nb, cudaMemcpyDefault, ctx->stream));
+        CU(ctx, cudaMemcpyAsync(m->z, z, nb, cudaMemcpyDefault, ctx->stream));
     }
-    if (m->ntri) CU(ctx, cudaMemcpyAsync(m->rgb, rgb, 3 * (size_t)m->ntri, cudaMemcpyHostToDevice, ctx->stream));
+    if (m->ntri) CU(ctx, cudaMemcpyAsync(m->rgb, rgb, 3 * (size_t)m->ntri, cudaMemcpyDefault, ctx->stream));
     return SLOTH_OK;
 }
 

@@ -69,6 +69,9 @@ SIGNATURES = {
     "sloth_batch_fragments": (C.c_int, [_vp, _u64p]),
     "sloth_batch_set_tile_shape": (C.c_int, [_vp, C.c_int]),
     "sloth_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+    "sloth_batch_depth_cells": (C.c_int, [_vp, C.c_uint32, _u64p, _u64p]),
+    "sloth_batch_shade": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int]),
+    "sloth_batch_shade_backward": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sloth_ctx_set_timing": (C.c_int, [_vp, C.c_int]),
     "sloth_ctx_kernel_time": (C.c_int, [_vp, C.c_char_p, C.POINTER(C.c_double), _u64p]),
     "sloth_ctx_launch_count": (C.c_uint64, [_vp]),
@@ -153,6 +156,7 @@ class Context:
         if st != OK:
             raise SlothError(st, "sloth_ctx_create failed (no CUDA device?)")
         self.h = h
+        self.device = device
         self.width = self.height = 0
         self.image = False
 
@@ -262,12 +266,20 @@ class Mesh:
         ctx._check(st)
         self.h = h
         self.ntri = ntri
+        self.nvert = x.size
 
     def update(self, x, y, z, rgb):
         """Overwrite positions and colours in place (async; keep the arrays alive)."""
         self._keep = (x, y, z, rgb)
         st = self.lib.sloth_mesh_update(self.h, _ptr(x, C.c_float), _ptr(y, C.c_float), _ptr(z, C.c_float),
                                         _ptr(rgb, C.c_uint8))
+        self.ctx._check(st)
+
+    def update_device(self, x: int, y: int, z: int, rgb: int):
+        """Overwrite positions and colours from device pointers (ints), asynchronously on
+        the context's stream."""
+        fp, bp = C.POINTER(C.c_float), C.POINTER(C.c_uint8)
+        st = self.lib.sloth_mesh_update(self.h, C.cast(x, fp), C.cast(y, fp), C.cast(z, fp), C.cast(rgb, bp))
         self.ctx._check(st)
 
     @property
@@ -377,6 +389,23 @@ class Batch:
         s, ms = C.c_int(), C.c_float()
         self.ctx._check(self.lib.sloth_batch_autotune(self.h, reps, C.byref(s), C.byref(ms)))
         return s.value, ms.value
+
+    # ---- differentiable shading (device pointers as ints, e.g. torch data_ptr()) ----
+    def depth_cells(self, frame: int) -> tuple[int, int]:
+        """(first depth cell, count) of a frame in the shaded image's cell order."""
+        a, n = C.c_uint64(), C.c_uint64()
+        self.ctx._check(self.lib.sloth_batch_depth_cells(self.h, frame, C.byref(a), C.byref(n)))
+        return a.value, n.value
+
+    def shade(self, vertex_rgb: int, light: int, rgb: int, store_visibility: bool = True):
+        self.ctx._check(self.lib.sloth_batch_shade(self.h, C.c_void_p(vertex_rgb), C.c_void_p(light),
+                                                   C.c_void_p(rgb), 1 if store_visibility else 0))
+
+    def shade_backward(self, vertex_rgb: int, light: int, grad_rgb: int, grad_pos: int = 0,
+                       grad_vertex_rgb: int = 0, grad_light: int = 0):
+        self.ctx._check(self.lib.sloth_batch_shade_backward(
+            self.h, C.c_void_p(vertex_rgb), C.c_void_p(light), C.c_void_p(grad_rgb),
+            C.c_void_p(grad_pos or None), C.c_void_p(grad_vertex_rgb or None), C.c_void_p(grad_light or None)))
 
 
 def cells_to_text(cells: np.ndarray) -> str:

@@ -164,6 +164,13 @@ def displaced_icosphere(subdiv: int, seed: int, amplitude: float = 0.1, rgb=(200
     return _mesh(p32[:, 0], p32[:, 1], p32[:, 2], f, col)
 
 
+def vertex_colours(m: dict, seed: int, freq: float = 1.5) -> np.ndarray:
+    """(nvert, 3) f32 vertex colours in [0, 1]: one seeded value-noise field per channel."""
+    p = np.stack([m["x"], m["y"], m["z"]], 1).astype(np.float64)
+    c = np.stack([0.5 + 0.5 * value_noise3(p, seed + k, freq) for k in range(3)], 1)
+    return np.clip(c, 0.0, 1.0).astype(np.float32)
+
+
 def cli_rotation(yaw: float = 0.0, pitch: float = 0.0, roll: float = 0.0) -> tuple[float, float, float]:
     """The Euler angles (roll, pitch, yaw slots of from_euler_angles) that the CLI builds
     from `-x/--yaw`, `-y/--pitch`, `-z/--roll` (src/inputs.rs:131-149): the yaw flag feeds
