@@ -278,7 +278,7 @@ def run_gpu(args):
     launches = ctx.launch_count() - launches0
     ms = sum(a.elapsed_time(b) for a, b in evs)
     kernels = {}
-    for name in ("vertex", "setup", "newline", "bin_count_large", "bin_scan", "bin_fill", "bin_fill_large", "raster", "resolve"):
+    for name in ("vertex", "setup", "newline", "bin_count_large", "bin_scan", "bin_fill", "bin_fill_large", "bin_items", "raster", "resolve"):
         t, n = ctx.kernel_time(name)
         if n:
             kernels[name] = {"ms_per_launch": t / n, "launches": n}
@@ -591,11 +591,13 @@ def run_config4(torch, stream, device, args):
 CONFIG5 = ("config5: fit vertex colours and positions of an icosphere subdivision 4 (5,120 triangles, initial "
            "colours 0.5) to 64 views at 256x256 of a displaced icosphere subdivision 6 (noise amplitude 0.1, "
            "value-noise vertex colours), 200 Adam steps (lr 1e-2), light (0.577, 0.577, 0.577)")
+CONFIG5_LAPLACIAN = 1e5      # weight of sum(|L p|^2), uniform mesh Laplacian on the fitted positions
 
 
 def run_config5(torch, stream, device, args, steps=200):
     """Inverse rendering: Adam on vertex positions and colours through the differentiable
-    path, visibility stored (it fits the 1 GB budget) and recomputed."""
+    path (loss = sum of squared image differences + a uniform-Laplacian smoothness term on
+    the positions), visibility stored (it fits the 1 GB budget) and recomputed."""
     import diff_render as DR
     import sloth_gpu as S
     import workloads as W
@@ -612,10 +614,13 @@ def run_config5(torch, stream, device, args, steps=200):
     tp = torch.from_numpy(np.stack([tgt["x"], tgt["y"], tgt["z"]], 1).astype(np.float32)).to(dev)
     target = DR.shade_views(tp, torch.from_numpy(tcol).to(dev), light, sv_t).detach().clone()
     sv_t.close()
-    out = {"workload": CONFIG5, "views": len(views), "steps": steps}
     p0 = np.stack([fit["x"], fit["y"], fit["z"]], 1).astype(np.float32)
-    for store in (None, False):
-        sv = DR.ShadedViews(ctx, fit, views, stream, store_visibility=store, vis_budget_bytes=1 << 30)
+    lap = DR.uniform_laplacian(fit["idx"], p0.shape[0], dev)
+    out = {"workload": CONFIG5, "views": len(views), "steps": steps,
+           "loss": f"sum((rgb - target)^2) + {CONFIG5_LAPLACIAN:g} * sum(|L p|^2), L the uniform mesh Laplacian",
+           "rmse": "over every depth cell and channel of the 64 views (background included)"}
+
+    def optimise(sv, nsteps, timed):
         pos = torch.from_numpy(p0).to(dev).requires_grad_(True)
         col = torch.full((p0.shape[0], 3), 0.5, dtype=torch.float32, device=dev, requires_grad=True)
         opt = torch.optim.Adam([pos, col], lr=1e-2)
@@ -629,18 +634,23 @@ def run_config5(torch, stream, device, args, steps=200):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         a.record(stream)
-        for _ in range(steps):
+        for _ in range(nsteps):
             opt.zero_grad(set_to_none=True)
-            loss = ((DR.shade_views(pos, col, light, sv) - target) ** 2).sum()
+            loss = ((DR.shade_views(pos, col, light, sv) - target) ** 2).sum() + CONFIG5_LAPLACIAN * (lap(pos) ** 2).sum()
             loss.backward()
             opt.step()
         b.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-        key = "stored" if sv.store_visibility else "recomputed"
-        out[key] = {"steps_per_s": steps / wall, "device_ms_per_step": a.elapsed_time(b) / steps,
-                    "rmse_initial": r0, "rmse_final": rmse(),
-                    "visibility_bytes": sv.ncells * DR.ShadedViews.VIS_BYTES_PER_CELL if sv.store_visibility else 0}
+        return {"steps_per_s": nsteps / wall, "device_ms_per_step": a.elapsed_time(b) / nsteps,
+                "rmse_initial": r0, "rmse_final": rmse()}
+
+    for store in (None, False):
+        sv = DR.ShadedViews(ctx, fit, views, stream, store_visibility=store, vis_budget_bytes=1 << 30)
+        optimise(sv, 5, False)                     # warm-up (first-use costs of every kernel)
+        r = optimise(sv, steps, True)
+        r["visibility_bytes"] = sv.ncells * DR.ShadedViews.VIS_BYTES_PER_CELL if sv.store_visibility else 0
+        out["stored" if sv.store_visibility else "recomputed"] = r
         sv.close()
     torch.cuda.synchronize()
     ctx.close()

@@ -56,7 +56,11 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_setup_kernel(BatchDev 
     const BatchFrame &f = b.frames[d.frame];
     const uint32_t t = (uint32_t)blk.y + threadIdx.x;
     bool large = false;
-    if (t < d.mesh.ntri) {
+    const bool live = t < d.mesh.ntri;
+    TriRecord r;
+    TileSpan sp{};
+    const Viewport vp = vp_batch(f.g);
+    if (live) {
         uint32_t i1, i2, i3;
         if (d.mesh.idx) {
             i1 = __ldg(d.mesh.idx + 3 * (size_t)t + 0);
@@ -66,14 +70,13 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_setup_kernel(BatchDev 
             i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
         }
         const float4 *tv = b.tv + d.vert_off;
-        const TriRecord r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3),
-                                         d.mesh.rgb + 3 * (size_t)t, f.g.w, f.g.h);
+        r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), d.mesh.rgb + 3 * (size_t)t, f.g.w,
+                         f.g.h);
         f.fb.records[d.local_base + t] = r;
-        const Viewport vp = vp_batch(f.g);
-        const TileSpan sp = tile_span(vp, r);
+        sp = tile_span(vp, r);
         large = sp.large;
-        if (!large) count_small_tiles(r, vp, sp, b.bb.tile_count + f.tile_off);
     }
+    count_small_tiles_warp(live && !large, r, vp, sp, b.bb.tile_count + f.tile_off);
     const unsigned m = __ballot_sync(0xffffffffu, large);
     if (m) {
         const int lane = threadIdx.x & 31;
@@ -140,54 +143,79 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_fill_kernel(BatchDev b
     const int2 blk = blocks[blockIdx.x];
     const BatchDraw &d = b.draws[blk.x];
     const uint32_t t = (uint32_t)blk.y + threadIdx.x;
-    if (t >= d.mesh.ntri) return;
     const BatchFrame &f = b.frames[d.frame];
     const uint32_t gtri = d.local_base + t;
-    const TriRecord r = f.fb.records[gtri];
     const Viewport vp = vp_batch(f.g);
-    const TileSpan sp = tile_span(vp, r);
-    if (sp.large || sp.ntiles == 0) return;
-    fill_small(r, gtri, vp, sp, b.bb.tile_cursor + f.tile_off, b.bb.entries, b.bb.capacity);
+    const bool live = t < d.mesh.ntri;
+    TriRecord r;
+    TileSpan sp{};
+    if (live) {
+        r = f.fb.records[gtri];
+        sp = tile_span(vp, r);
+    }
+    fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, b.bb.tile_cursor + f.tile_off,
+                    b.bb.entries, b.bb.capacity);
 }
 
-// Raster over every frame's tiles in one launch: each CTA takes one (frame, tile) item
-// from a device-side queue (warp 0 pulls items until it gets a non-empty tile) and
-// rasterizes it; the hardware block scheduler keeps the SMs fed as CTAs finish.  A CTA
-// handles exactly one item: in a CTA that looped over several items, warps were seen to
-// run ahead into a further pass over the same tile (barrier phases out of step) and to
-// overwrite its finished keys, so the loop is left to the block scheduler.
+__device__ __forceinline__ uint32_t frame_of_tile(const BatchDev &b, uint32_t tile)
+{
+    // last frame whose first tile is <= tile
+    uint32_t lo = 0, hi = b.nframes;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (b.frame_tile_off[mid] <= tile) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// One thread per global tile: the tile's raster items (tile, slice); a tile rasterized in
+// slices gets its keys cleared and its generation set first (bin_items_kernel, per frame).
+__global__ void __launch_bounds__(256) batch_items_kernel(BatchDev b)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= b.total_tiles) return;
+    const uint32_t nt = b.total_tiles;
+    const SplitParams sp{b.bb.slice_offset[nt + 1], b.bb.slice_offset[nt + 2]};
+    const uint32_t cnt = b.bb.tile_count[t], ns = tile_slices(cnt, sp);
+    const bool split = cnt > sp.threshold;
+    const uint32_t off = b.bb.slice_offset[t] + (split ? 0u : b.bb.slice_offset[nt + 3]);
+    for (uint32_t k = 0; k < ns && off + k < b.bb.item_capacity; ++k) b.bb.items[off + k] = make_uint2(t, k);
+    if (split) {
+        const BatchFrame &f = b.frames[frame_of_tile(b, t)];
+        const uint32_t lt = t - f.tile_off;
+        if (f.fb.tile_gen[lt] != f.fb.gen) {
+            const int tr = (int)lt / f.g.ntx, tc = (int)lt - tr * f.g.ntx;
+            unsigned long long *k0 = reinterpret_cast<unsigned long long *>(f.fb.keys) +
+                                     (size_t)tr * f.g.th * f.g.pitch + (size_t)tc * f.g.tw;
+            for (int r = 0; r < f.g.th; ++r)
+                for (int c = 0; c < f.g.tw; ++c) k0[(size_t)r * f.g.pitch + c] = kEmptyKey;
+            f.fb.tile_gen[lt] = f.fb.gen;
+        }
+    }
+}
+
+// Raster over every frame's tiles in one launch: CTA i rasterizes raster item i (a tile,
+// or a slice of a split tile) of the item list built by batch_items_kernel; the hardware
+// block scheduler keeps the SMs fed as CTAs finish.  CTAs past the item count return.
 template <int TW, int TH>
 __global__ void __launch_bounds__(kRasterThreads) batch_raster_kernel(BatchDev b)
 {
     __shared__ TileSmem<TW, TH> S;
-    __shared__ uint32_t s_item;
     if (b.bb.tile_offset[b.total_tiles] > b.bb.capacity) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *b.overflow = 1;
         return;
     }
-    if (threadIdx.x < 32) {
-        uint32_t it = 0;
-        for (;;) {
-            if (threadIdx.x == 0) it = atomicAdd(b.queue_head, 1u);
-            it = __shfl_sync(0xffffffffu, it, 0);
-            if (it >= b.total_tiles || b.bb.tile_count[it] != 0) break;
-        }
-        if (threadIdx.x == 0) s_item = it;
-        __syncwarp();
-    }
-    block_sync();
-    const uint32_t item = s_item;
-    if (item >= b.total_tiles) return;
-    // frame of the global tile: last frame whose first tile is <= item
-    uint32_t lo = 0, hi = b.nframes;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (b.frame_tile_off[mid] <= item) lo = mid;
-        else hi = mid;
-    }
-    const BatchFrame &f = b.frames[lo];
-    raster_tile<TW, TH>(S, f.g, f.fb, (int)(item - f.tile_off), b.bb.tile_count[item],
-                        b.bb.entries + b.bb.tile_offset[item], b.depth_cull);
+    if (blockIdx.x >= b.bb.slice_offset[b.total_tiles] || blockIdx.x >= b.bb.item_capacity) return;
+    const uint2 it = b.bb.items[blockIdx.x];
+    const BatchFrame &f = b.frames[frame_of_tile(b, it.x)];
+    const uint32_t all = b.bb.tile_count[it.x];
+    const uint32_t thr = b.bb.slice_offset[b.total_tiles + 1], slice = b.bb.slice_offset[b.total_tiles + 2];
+    const bool split = all > thr;
+    const uint32_t first = split ? it.y * slice : 0u;
+    const uint32_t cnt = split ? min(slice, all - first) : all;
+    raster_tile<TW, TH>(S, f.g, f.fb, (int)(it.x - f.tile_off), cnt, b.bb.entries + b.bb.tile_offset[it.x] + first,
+                        b.depth_cull, split);
 }
 
 // blocks[i] = (frame, first cell).
@@ -248,8 +276,8 @@ cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nb
 cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, cudaStream_t s)
 {
     if (!b.total_tiles) return cudaSuccess;
-    // one CTA per queue item (a CTA whose pulls only find empty tiles exits at once)
-    const uint32_t grid = b.total_tiles;
+    // one CTA per possible raster item; CTAs past the item count exit at once
+    const uint32_t grid = b.bb.item_capacity;
 #define SLOTH_BATCH_RASTER_CASE(W_, H_)                                                        \
     if (tw == W_ && th == H_) {                                                                \
         batch_raster_kernel<W_, H_><<<grid, kRasterThreads, 0, s>>>(b);                        \
@@ -258,6 +286,13 @@ cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, cudaStream_t 
     SLOTH_TILE_SHAPES(SLOTH_BATCH_RASTER_CASE)
 #undef SLOTH_BATCH_RASTER_CASE
     return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_batch_items(const BatchDev &b, cudaStream_t s)
+{
+    if (!b.total_tiles) return cudaSuccess;
+    batch_items_kernel<<<(b.total_tiles + 255) / 256, 256, 0, s>>>(b);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_batch_resolve(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s)

@@ -53,7 +53,6 @@ struct sloth_batch {
     BinBuffers bb{};
     size_t entries_cap = 0;
     uint32_t *large_frame = nullptr;
-    uint32_t *queue_head = nullptr;
     uint32_t *overflow = nullptr;
     uint32_t *h_total = nullptr;              // pinned
     uint32_t *h_overflow = nullptr;           // pinned
@@ -134,7 +133,9 @@ void free_layout(sloth_batch *b)
     bfree(b->bb.large_queue);
     bfree(b->bb.large_count);
     bfree(b->large_frame);
-    bfree(b->queue_head);
+    bfree(b->bb.slice_offset);
+    bfree(b->bb.items);
+    b->bb.item_capacity = 0;
     bfree(b->overflow);
     for (auto &p : b->blk) bfree(p);
     b->entries_cap = 0;
@@ -252,7 +253,7 @@ sloth_status build(sloth_batch *b, int shape)
     BCU(b, balloc(&b->bb.large_queue, rec));
     BCU(b, balloc(&b->bb.large_count, 1));
     BCU(b, balloc(&b->large_frame, rec));
-    BCU(b, balloc(&b->queue_head, 1));
+    BCU(b, balloc(&b->bb.slice_offset, tiles + 4));
     BCU(b, balloc(&b->overflow, 1));
     BCU(b, balloc(&b->d_mats, nd));
     for (uint32_t f = 0; f < nf; ++f) {
@@ -296,7 +297,6 @@ BatchDev dev_view(sloth_batch *b)
     d.bb = b->bb;
     d.bb.capacity = (uint32_t)(b->entries_cap > 0xffffffffu ? 0xffffffffu : b->entries_cap);
     d.large_frame = b->large_frame;
-    d.queue_head = b->queue_head;
     d.overflow = b->overflow;
     d.depth_cull = sloth_ctx_depth_cull(b->ctx);
     return d;
@@ -311,7 +311,6 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     if ((e = cudaMemsetAsync(b->nltree, 0xff, (size_t)b->total_nl * 4, s))) return e;
     if ((e = cudaMemsetAsync(b->bb.large_count, 0, 4, s))) return e;
     if ((e = cudaMemsetAsync(b->fragments, 0, 8, s))) return e;
-    if ((e = cudaMemsetAsync(b->queue_head, 0, 4, s))) return e;
     if ((e = cudaMemsetAsync(b->overflow, 0, 4, s))) return e;
     if ((e = cudaMemcpyAsync(b->d_mats, b->h_mats, b->meshes.size() * sizeof(Mat4), cudaMemcpyHostToDevice, s)))
         return e;
@@ -328,6 +327,7 @@ cudaError_t enqueue_back(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     cudaError_t e;
     if ((e = launch_batch_fill(d, b->blk[1], b->nblk[1], s))) return e;
     if ((e = launch_batch_bin_large(d, true, s))) return e;
+    if ((e = launch_batch_items(d, s))) return e;
     const int tw = kTileShapes[b->shape][0], th = kTileShapes[b->shape][1];
     if ((e = launch_batch_raster(d, tw, th, s))) return e;
     return launch_batch_resolve(d, b->blk[3], b->nblk[3], s);
@@ -348,9 +348,12 @@ sloth_status render_planned(sloth_batch *b)
             b->graph = nullptr;
         }
         bfree(b->bb.entries);
+        bfree(b->bb.items);
         const size_t cap = need + need / 4 + 1024;   // headroom for other transforms
         BCU(b, balloc(&b->bb.entries, cap));
         b->entries_cap = cap;
+        b->bb.item_capacity = raster_item_bound(b->total_tiles, cap);
+        BCU(b, balloc(&b->bb.items, b->bb.item_capacity));
         d = dev_view(b);
     }
     BCU(b, enqueue_back(b, d, s));

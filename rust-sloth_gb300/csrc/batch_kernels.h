@@ -42,7 +42,6 @@ struct BatchDev {
     const uint32_t *frame_tile_off;   // nframes + 1 (for tile -> frame lookups)
     BinBuffers bb;             // global tile arrays and entries
     uint32_t *large_frame;     // frame of each large-queue entry
-    uint32_t *queue_head;      // raster work queue
     uint32_t *overflow;        // set when the entries outgrew their capacity
     int depth_cull;
 };
@@ -54,6 +53,7 @@ cudaError_t launch_batch_newline(const BatchDev &b, const int2 *blocks, uint32_t
                                  cudaStream_t s);
 cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s);
 cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s);
+cudaError_t launch_batch_items(const BatchDev &b, cudaStream_t s);
 cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, cudaStream_t s);
 cudaError_t launch_batch_resolve(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s);
 cudaError_t prepare_batch_kernels();

@@ -31,42 +31,161 @@ bin_large_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
     }
 }
 
-// Exclusive scan of tile counts by one block; offsets[n] = total; cursors = offsets.
+__device__ __forceinline__ SplitParams split_params(const BinBuffers &bb, uint32_t n)
+{
+    return SplitParams{bb.slice_offset[n + 1], bb.slice_offset[n + 2]};
+}
+
+// Exclusive scans of the tile entry counts (offsets, cursors; offsets[n] = total) and of
+// the raster items per tile, by one block, 4096 tiles per step with running carries.  A
+// first pass sets the split threshold from the mean entries of a non-empty tile; the
+// items of split tiles are numbered first (slice_offset counts them apart; the item
+// kernel adds the split tiles' item count to the others').
 __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers bb)
 {
-    __shared__ uint32_t warp_sums[32];
+    __shared__ unsigned long long red_e[32];
+    __shared__ uint32_t red_t[32];
+    __shared__ uint32_t ws_e[32], ws_h[32], ws_l[32];
+    __shared__ uint32_t carry_e, carry_h, carry_l;
+    __shared__ SplitParams sp_s;
     const uint32_t tid = threadIdx.x;
-    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
-    const uint32_t lo = min(n, tid * per), hi = min(n, lo + per);
-    uint32_t local = 0;
-    for (uint32_t i = lo; i < hi; ++i) local += bb.tile_count[i];
-    // inclusive scan of `local` across the block
     const int lane = tid & 31, wid = tid >> 5;
-    uint32_t v = local;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        uint32_t o = __shfl_up_sync(0xffffffffu, v, d);
-        if (lane >= d) v += o;
+    // pass 1: entries and non-empty tiles
+    unsigned long long se = 0;
+    uint32_t st = 0;
+    for (uint32_t i = tid; i < n; i += blockDim.x) {
+        const uint32_t c = bb.tile_count[i];
+        se += c;
+        st += c != 0u;
     }
-    if (lane == 31) warp_sums[wid] = v;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        se += __shfl_xor_sync(0xffffffffu, se, d);
+        st += __shfl_xor_sync(0xffffffffu, st, d);
+    }
+    if (lane == 0) {
+        red_e[wid] = se;
+        red_t[wid] = st;
+    }
+    if (tid == 0) carry_e = carry_h = carry_l = 0;
     block_sync();
-    if (wid == 0) {
-        uint32_t s = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0u;
+    if (tid == 0) {
+        unsigned long long te = 0;
+        uint32_t tt = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            te += red_e[w];
+            tt += red_t[w];
+        }
+        const unsigned long long mean = (te + (tt ? tt : 1u) - 1) / (tt ? tt : 1u);
+        // 4x the mean, but low enough that a launch of few tiles still yields about
+        // kTargetItems items to spread over the GPU
+        unsigned long long thr = mean * 4 < 2 * te / kTargetItems ? mean * 4 : 2 * te / kTargetItems;
+        if (thr < kMinSplitEntries) thr = kMinSplitEntries;
+        sp_s.threshold = (uint32_t)(thr < 0x40000000ull ? thr : 0x40000000ull);
+        sp_s.slice = sp_s.threshold / 2;
+    }
+    block_sync();
+    const SplitParams sp = sp_s;
+    // pass 2: the scans
+    for (uint32_t base = 0; base < n; base += 4 * 1024) {
+        const uint32_t i0 = base + 4 * tid;
+        uint32_t c[4], hs[4], ls[4], le = 0, lh = 0, ll = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            c[k] = i0 + k < n ? bb.tile_count[i0 + k] : 0u;
+            const uint32_t ns = tile_slices(c[k], sp);
+            hs[k] = c[k] > sp.threshold ? ns : 0u;
+            ls[k] = c[k] > sp.threshold ? 0u : ns;
+            le += c[k];
+            lh += hs[k];
+            ll += ls[k];
+        }
+        uint32_t ve = le, vh = lh, vl = ll;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            uint32_t o = __shfl_up_sync(0xffffffffu, s, d);
-            if (lane >= d) s += o;
+            const uint32_t oe = __shfl_up_sync(0xffffffffu, ve, d), oh = __shfl_up_sync(0xffffffffu, vh, d),
+                           ol = __shfl_up_sync(0xffffffffu, vl, d);
+            if (lane >= d) {
+                ve += oe;
+                vh += oh;
+                vl += ol;
+            }
         }
-        warp_sums[lane] = s;
+        if (lane == 31) {
+            ws_e[wid] = ve;
+            ws_h[wid] = vh;
+            ws_l[wid] = vl;
+        }
+        block_sync();
+        if (wid == 0) {
+            uint32_t a = ws_e[lane], b = ws_h[lane], d3 = ws_l[lane];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t oa = __shfl_up_sync(0xffffffffu, a, d), ob = __shfl_up_sync(0xffffffffu, b, d),
+                               oc = __shfl_up_sync(0xffffffffu, d3, d);
+                if (lane >= d) {
+                    a += oa;
+                    b += ob;
+                    d3 += oc;
+                }
+            }
+            ws_e[lane] = a;
+            ws_h[lane] = b;
+            ws_l[lane] = d3;
+        }
+        block_sync();
+        uint32_t pe = carry_e + ve - le + (wid > 0 ? ws_e[wid - 1] : 0u);
+        uint32_t ph = carry_h + vh - lh + (wid > 0 ? ws_h[wid - 1] : 0u);
+        uint32_t pl = carry_l + vl - ll + (wid > 0 ? ws_l[wid - 1] : 0u);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i0 + k < n) {
+                bb.tile_offset[i0 + k] = pe;
+                bb.tile_cursor[i0 + k] = pe;
+                bb.slice_offset[i0 + k] = c[k] > sp.threshold ? ph : pl;
+            }
+            pe += c[k];
+            ph += hs[k];
+            pl += ls[k];
+        }
+        block_sync();                    // every thread has read the carries
+        if (tid == blockDim.x - 1) {
+            carry_e = pe;
+            carry_h = ph;
+            carry_l = pl;
+        }
+        block_sync();
     }
-    block_sync();
-    uint32_t run = v - local + (wid > 0 ? warp_sums[wid - 1] : 0u);   // exclusive prefix
-    for (uint32_t i = lo; i < hi; ++i) {
-        bb.tile_offset[i] = run;
-        bb.tile_cursor[i] = run;
-        run += bb.tile_count[i];
+    if (tid == 0) {
+        bb.tile_offset[n] = carry_e;
+        bb.slice_offset[n] = carry_h + carry_l;
+        bb.slice_offset[n + 1] = sp.threshold;
+        bb.slice_offset[n + 2] = sp.slice;
+        bb.slice_offset[n + 3] = carry_h;
     }
-    if (tid == blockDim.x - 1) bb.tile_offset[n] = warp_sums[(blockDim.x >> 5) - 1];
+}
+
+// One thread per tile: the raster items (tile, slice) of the tile, and for a tile that is
+// rasterized in slices, its keys cleared (unless they hold keys of earlier draws since
+// the clear) and its generation set before the slices fold into them.
+__global__ void __launch_bounds__(256)
+bin_items_kernel(uint32_t n, FrameGeom g, FrameBuffers fb, BinBuffers bb)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const SplitParams sp = split_params(bb, n);
+    const uint32_t cnt = bb.tile_count[t], ns = tile_slices(cnt, sp);
+    const bool split = cnt > sp.threshold;
+    const uint32_t off = bb.slice_offset[t] + (split ? 0u : bb.slice_offset[n + 3]);
+    for (uint32_t k = 0; k < ns && off + k < bb.item_capacity; ++k) bb.items[off + k] = make_uint2(t, k);
+    if (split && fb.tile_gen[t] != fb.gen) {
+        const int tr = (int)t / g.ntx, tc = (int)t - tr * g.ntx;
+        unsigned long long *k0 = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)tr * g.th * g.pitch +
+                                 (size_t)tc * g.tw;
+        for (int r = 0; r < g.th; ++r)
+            for (int c = 0; c < g.tw; ++c) k0[(size_t)r * g.pitch + c] = kEmptyKey;
+        fb.tile_gen[t] = fb.gen;
+    }
 }
 
 // One thread per triangle of the draw: small triangles write their tile entries.
@@ -74,13 +193,16 @@ __global__ void __launch_bounds__(256)
 bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntri) return;
     const uint32_t gtri = tri_base + t;
-    const TriRecord r = fb.records[gtri];
     const Viewport vp = vp_of(g);
-    const TileSpan sp = tile_span(vp, r);
-    if (sp.large || sp.ntiles == 0) return;
-    fill_small(r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
+    const bool live = t < ntri;
+    TriRecord r;
+    TileSpan sp{};
+    if (live) {
+        r = fb.records[gtri];
+        sp = tile_span(vp, r);
+    }
+    fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
 }
 
 static int large_grid()
@@ -98,6 +220,14 @@ cudaError_t launch_bin_count_large(uint32_t tri_base, const FrameGeom &g, const 
 cudaError_t launch_bin_scan(uint32_t ntiles, const BinBuffers &bb, cudaStream_t s)
 {
     bin_scan_kernel<<<1, 1024, 0, s>>>(ntiles, bb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_items(uint32_t ntiles, const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
+                             cudaStream_t s)
+{
+    if (ntiles == 0) return cudaSuccess;
+    bin_items_kernel<<<(ntiles + 255) / 256, 256, 0, s>>>(ntiles, g, fb, bb);
     return cudaGetLastError();
 }
 

@@ -59,24 +59,45 @@ __device__ __forceinline__ void bin_large_warp(const TriRecord &r, uint32_t gtri
     }
 }
 
-// One thread writes a small triangle's entries.
-__device__ __forceinline__ void fill_small(const TriRecord &r, uint32_t gtri, const Viewport &vp,
-                                           const TileSpan &sp, uint32_t *tile_cursor, uint64_t *entries,
-                                           uint32_t capacity)
+// Writes a small triangle's entries.  Called by all 32 lanes (lanes with active false
+// write nothing); each lane's first tile takes its slots with one atomic per distinct
+// tile of the warp, like count_small_tiles_warp.
+__device__ __forceinline__ void fill_small_warp(bool active, const TriRecord &r, uint32_t gtri, const Viewport &vp,
+                                                const TileSpan &sp, uint32_t *tile_cursor, uint64_t *entries,
+                                                uint32_t capacity)
 {
-    auto put = [&](int tr, int tc) {
-        const bool wrapped = !sp.W.empty() && !clip_wrapped(vp, sp.W, tr, tc).empty();
-        const uint32_t slot = atomicAdd(&tile_cursor[tr * vp.ntx + tc], 1u);
-        if (slot < capacity) entries[slot] = entry_key(r.zlo, gtri, wrapped);
-    };
-    for (int tr = sp.TU.ya; tr < sp.TU.yb; ++tr)
-        for (int tc = sp.TU.xa; tc < sp.TU.xb; ++tc)
-            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
-    for (int tr = sp.TW.ya; tr < sp.TW.yb; ++tr)
-        for (int tc = sp.TW.xa; tc < sp.TW.xb; ++tc) {
-            if (in_rect(sp.TU, tr, tc)) continue;
-            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
-        }
+    uint32_t first = 0xffffffffu;
+    bool first_wrapped = false;
+    if (active) {
+        auto put = [&](int tr, int tc) {
+            const bool wrapped = !sp.W.empty() && !clip_wrapped(vp, sp.W, tr, tc).empty();
+            const uint32_t tile = tr * vp.ntx + tc;
+            if (first == 0xffffffffu) {
+                first = tile;
+                first_wrapped = wrapped;
+                return;
+            }
+            const uint32_t slot = atomicAdd(&tile_cursor[tile], 1u);
+            if (slot < capacity) entries[slot] = entry_key(r.zlo, gtri, wrapped);
+        };
+        for (int tr = sp.TU.ya; tr < sp.TU.yb; ++tr)
+            for (int tc = sp.TU.xa; tc < sp.TU.xb; ++tc)
+                if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
+        for (int tr = sp.TW.ya; tr < sp.TW.yb; ++tr)
+            for (int tc = sp.TW.xa; tc < sp.TW.xb; ++tc) {
+                if (in_rect(sp.TU, tr, tc)) continue;
+                if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
+            }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, first);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (first != 0xffffffffu && lane == leader) base = atomicAdd(&tile_cursor[first], (uint32_t)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (first != 0xffffffffu) {
+        const uint32_t slot = base + __popc(peers & ((1u << lane) - 1u));
+        if (slot < capacity) entries[slot] = entry_key(r.zlo, gtri, first_wrapped);
+    }
 }
 
 }  // namespace sloth

@@ -4,25 +4,31 @@
 
 namespace sloth {
 
+// One CTA per raster item (tile, slice); CTAs past the item count return at once.
 template <int TW, int TH>
 __global__ void __launch_bounds__(kRasterThreads)
-raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb, int depth_cull)
+raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb, uint32_t ntiles, int depth_cull)
 {
     __shared__ TileSmem<TW, TH> S;
-    const int tile = blockIdx.x;
-    const uint32_t cnt = bb.tile_count[tile];
-    if (cnt == 0) return;
-    raster_tile<TW, TH>(S, g, fb, tile, cnt, bb.entries + bb.tile_offset[tile], depth_cull);
+    if (blockIdx.x >= bb.slice_offset[ntiles] || blockIdx.x >= bb.item_capacity) return;
+    const uint2 it = bb.items[blockIdx.x];
+    const uint32_t all = bb.tile_count[it.x];
+    const uint32_t thr = bb.slice_offset[ntiles + 1], slice = bb.slice_offset[ntiles + 2];
+    const bool split = all > thr;
+    const uint32_t first = split ? it.y * slice : 0u;
+    const uint32_t cnt = split ? min(slice, all - first) : all;
+    raster_tile<TW, TH>(S, g, fb, (int)it.x, cnt, bb.entries + bb.tile_offset[it.x] + first, depth_cull, split);
 }
 
 cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
                           int depth_cull, cudaStream_t s)
 {
-    const int ntiles = g.ntx * g.nty;
+    const uint32_t ntiles = (uint32_t)(g.ntx * g.nty);
     if (ntiles == 0) return cudaSuccess;
+    const uint32_t grid = bb.item_capacity;
 #define SLOTH_RASTER_CASE(W_, H_)                                                              \
     if (g.tw == W_ && g.th == H_) {                                                            \
-        raster_kernel<W_, H_><<<ntiles, kRasterThreads, 0, s>>>(g, fb, bb, depth_cull);        \
+        raster_kernel<W_, H_><<<grid, kRasterThreads, 0, s>>>(g, fb, bb, ntiles, depth_cull);  \
         return cudaGetLastError();                                                             \
     }
     SLOTH_TILE_SHAPES(SLOTH_RASTER_CASE)

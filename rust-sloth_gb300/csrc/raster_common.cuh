@@ -106,15 +106,17 @@ __device__ __forceinline__ void tile_zmax(const unsigned long long *skeys, int R
 }
 
 // Rasterize one tile of one frame: `cnt` entries at `entries`.  Called by all threads of
-// the CTA; returns after the tile's keys are stored and its generation is set.
+// the CTA; returns after the tile's keys are stored and its generation is set.  A slice
+// of a split tile (split true) starts from empty keys and folds its keys into the tile's
+// with a global atomicMin; the tile's keys and generation were prepared before the launch.
 template <int TW, int TH>
 __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom &g, const FrameBuffers &fb,
                                             int tile, uint32_t cnt, const uint64_t *__restrict__ entries,
-                                            int depth_cull)
+                                            int depth_cull, bool split = false)
 {
     const int tr = tile / g.ntx, tc = tile - (tile / g.ntx) * g.ntx;
     const int R0 = tr * TH, C0 = tc * TW;
-    const bool merge = fb.tile_gen[tile] == fb.gen;
+    const bool merge = !split && fb.tile_gen[tile] == fb.gen;
     unsigned long long *gk = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)R0 * g.pitch + C0;
     for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
         const int rr = i / TW, cc = i - rr * TW;
@@ -192,7 +194,11 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
     block_sync();
     for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
         const int rr = i / TW, cc = i - rr * TW;
-        gk[(size_t)rr * g.pitch + cc] = S.keys[i];
+        if (!split) {
+            gk[(size_t)rr * g.pitch + cc] = S.keys[i];
+        } else if (S.keys[i] != kEmptyKey) {
+            atomicMin(&gk[(size_t)rr * g.pitch + cc], S.keys[i]);
+        }
     }
     if (threadIdx.x < 32) {
         // warp 0, converged: sum the per-warp counts, one atomic, tile generation
@@ -201,7 +207,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         for (int d = 16; d > 0; d >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, d);
         if (lane == 0) {
             atomicAdd(fb.fragments, (unsigned long long)tot);
-            fb.tile_gen[tile] = fb.gen;
+            if (!split) fb.tile_gen[tile] = fb.gen;
         }
         __syncwarp();
     }

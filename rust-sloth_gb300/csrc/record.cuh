@@ -142,17 +142,31 @@ __device__ __forceinline__ float row_dot(const float *m, float x, float y, float
 }
 
 // Count the small triangle's tiles (bin count pass).
-__device__ __forceinline__ void count_small_tiles(const TriRecord &r, const Viewport &vp, const TileSpan &sp,
-                                                  uint32_t *tile_count)
+// Adds 1 to the count of every tile a small triangle can write.  Called by all 32 lanes
+// (lanes with active false count nothing).  Each lane's first tile is counted with one
+// atomic per distinct tile of the warp: consecutive triangles of a mesh mostly share it.
+__device__ __forceinline__ void count_small_tiles_warp(bool active, const TriRecord &r, const Viewport &vp,
+                                                       const TileSpan &sp, uint32_t *tile_count)
 {
-    for (int tr = sp.TU.ya; tr < sp.TU.yb; ++tr)
-        for (int tc = sp.TU.xa; tc < sp.TU.xb; ++tc)
-            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) atomicAdd(&tile_count[tr * vp.ntx + tc], 1u);
-    for (int tr = sp.TW.ya; tr < sp.TW.yb; ++tr)
-        for (int tc = sp.TW.xa; tc < sp.TW.xb; ++tc) {
-            if (in_rect(sp.TU, tr, tc)) continue;
-            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) atomicAdd(&tile_count[tr * vp.ntx + tc], 1u);
-        }
+    uint32_t first = 0xffffffffu;
+    if (active) {
+        auto hit = [&](int tr, int tc) {
+            const uint32_t tile = tr * vp.ntx + tc;
+            if (first == 0xffffffffu) first = tile;
+            else atomicAdd(&tile_count[tile], 1u);
+        };
+        for (int tr = sp.TU.ya; tr < sp.TU.yb; ++tr)
+            for (int tc = sp.TU.xa; tc < sp.TU.xb; ++tc)
+                if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) hit(tr, tc);
+        for (int tr = sp.TW.ya; tr < sp.TW.yb; ++tr)
+            for (int tc = sp.TW.xa; tc < sp.TW.xb; ++tc) {
+                if (in_rect(sp.TU, tr, tc)) continue;
+                if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) hit(tr, tc);
+            }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, first);
+    if (first != 0xffffffffu && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+        atomicAdd(&tile_count[first], (uint32_t)__popc(peers));
 }
 
 }  // namespace sloth

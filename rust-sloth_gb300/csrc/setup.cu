@@ -56,6 +56,9 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, Fra
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = t < mesh.ntri;
     bool large = false;
+    TriRecord r;
+    TileSpan sp{};
+    const Viewport vp = to_vp(g);
     if (live) {
         uint32_t i1, i2, i3;
         if (mesh.idx) {
@@ -65,15 +68,13 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, Fra
         } else {
             i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
         }
-        const TriRecord r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3),
-                                         mesh.rgb + 3 * (size_t)t, g.w, g.h);
+        r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), mesh.rgb + 3 * (size_t)t, g.w, g.h);
         fb.records[tri_base + t] = r;
-        // binning: count tiles of small triangles here, queue the rest for warps
-        const Viewport vp = to_vp(g);
-        const TileSpan sp = tile_span(vp, r);
+        sp = tile_span(vp, r);
         large = sp.large;
-        if (!large) count_small_tiles(r, vp, sp, bb.tile_count);
     }
+    // binning: count tiles of small triangles here, queue the rest for warps
+    count_small_tiles_warp(live && !large, r, vp, sp, bb.tile_count);
     // warp-ballot compaction of the large-triangle queue
     const unsigned m = __ballot_sync(0xffffffffu, large);
     if (m) {

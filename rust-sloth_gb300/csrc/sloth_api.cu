@@ -156,6 +156,7 @@ static void free_frame(sloth_ctx *ctx)
     dfree(ctx->bb.tile_count);
     dfree(ctx->bb.tile_offset);
     dfree(ctx->bb.tile_cursor);
+    dfree(ctx->bb.slice_offset);
     ctx->have_frame = false;
     ctx->ntiles_cap = 0;
 }
@@ -189,6 +190,7 @@ static sloth_status alloc_frame(sloth_ctx *ctx)
     CU(ctx, dalloc(&ctx->bb.tile_count, ntiles));
     CU(ctx, dalloc(&ctx->bb.tile_offset, ntiles + 1));
     CU(ctx, dalloc(&ctx->bb.tile_cursor, ntiles));
+    CU(ctx, dalloc(&ctx->bb.slice_offset, ntiles + 4));
     ctx->ntiles_cap = (uint32_t)ntiles;
     ctx->fb.gen = 0;
     ctx->g = g;
@@ -379,6 +381,7 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     dfree(ctx->bb.entries);
     dfree(ctx->bb.large_queue);
     dfree(ctx->bb.large_count);
+    dfree(ctx->bb.items);
     dfree(ctx->tv);
     if (ctx->h_total) cudaFreeHost(ctx->h_total);
     if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
@@ -636,8 +639,12 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     size_t ecap = ctx->bb.capacity;
     if ((st = ensure_scratch(ctx, &ctx->bb.entries, &ecap, total)) != SLOTH_OK) return st;
     ctx->bb.capacity = (uint32_t)(ecap > 0xffffffffu ? 0xffffffffu : ecap);
+    size_t icap = ctx->bb.item_capacity;
+    if ((st = ensure_scratch(ctx, &ctx->bb.items, &icap, raster_item_bound(ntiles, total))) != SLOTH_OK) return st;
+    ctx->bb.item_capacity = (uint32_t)icap;
     CU(ctx, timed(ctx, "bin_fill", [&] { return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_fill_large", [&] { return launch_bin_fill_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+    CU(ctx, timed(ctx, "bin_items", [&] { return launch_bin_items(ntiles, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "raster", [&] { return launch_raster(g, ctx->fb, ctx->bb, ctx->depth_cull, s); }));
     ctx->tri_base += mesh->ntri;
     ctx->dirty = true;

@@ -41,7 +41,39 @@ struct BinBuffers {
     uint32_t capacity;
     uint32_t *large_queue;   // mesh-local triangle indices of triangles binned by warps
     uint32_t *large_count;   // 1
+    uint32_t *slice_offset;  // ntiles + 4: per tile the first raster item of its slices;
+                             // [ntiles] = items, [ntiles+1] = split threshold, [ntiles+2] =
+                             // slice size, [ntiles+3] = items of split tiles (listed first)
+    uint2 *items;            // item_capacity: (tile, slice) of each raster CTA
+    uint32_t item_capacity;
 };
+
+// A tile holding many more entries than the launch's mean is rasterized in slices by
+// separate CTAs, which fold their keys into the tile's with a 64-bit global atomicMin (the
+// minimum is order-independent, so the result is the same), and its slices are listed
+// before every other item so that they start first.  Without it a very dense small
+// viewport (hundreds of thousands of triangles over a few tiles) leaves a few CTAs working
+// long after the rest of the GPU is idle.  Split threshold: the smaller of 4 x the mean
+// entries of a non-empty tile and 2 x total / kTargetItems (so that a launch of few, evenly
+// heavy tiles still spreads over the GPU), at least kMinSplitEntries; slices hold half the
+// threshold.
+constexpr uint32_t kMinSplitEntries = 2048;
+constexpr uint32_t kTargetItems = 1024;
+
+struct SplitParams {
+    uint32_t threshold, slice;
+};
+
+__host__ __device__ inline uint32_t tile_slices(uint32_t n, SplitParams sp)
+{
+    return n == 0 ? 0u : (n <= sp.threshold ? 1u : (n + sp.slice - 1) / sp.slice);
+}
+
+// Raster CTAs needed for ntiles tiles holding at most `capacity` entries in total.
+inline uint32_t raster_item_bound(uint32_t ntiles, size_t capacity)
+{
+    return (uint32_t)(ntiles + capacity / (kMinSplitEntries / 2) + 1);
+}
 
 struct MeshDev {
     const float *x, *y, *z;  // nvert
@@ -69,6 +101,8 @@ cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
 cudaError_t launch_bin_count_large(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
                                    const BinBuffers &bb, cudaStream_t s);
 cudaError_t launch_bin_scan(uint32_t ntiles, const BinBuffers &bb, cudaStream_t s);
+cudaError_t launch_bin_items(uint32_t ntiles, const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
+                             cudaStream_t s);
 cudaError_t launch_bin_fill(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
                             const FrameBuffers &fb, const BinBuffers &bb, cudaStream_t s);
 cudaError_t launch_bin_fill_large(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,

@@ -108,3 +108,20 @@ def shade_views(pos: torch.Tensor, vrgb: torch.Tensor, light: torch.Tensor, view
     colours `vrgb` (nvert, 3) and light direction `light` (3,); differentiable in all
     three with the render's visibility held fixed."""
     return _ShadeFn.apply(pos, vrgb, light, views)
+
+
+def uniform_laplacian(idx: np.ndarray, nvert: int, device) -> "callable":
+    """p -> p - mean of p over each vertex's edge neighbours (the uniform mesh Laplacian),
+    for a smoothness term sum(|L p|^2) on fitted positions."""
+    f = np.asarray(idx, np.int64).reshape(-1, 3)
+    e = np.unique(np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), 1), axis=0)
+    src = torch.from_numpy(np.concatenate([e[:, 0], e[:, 1]])).to(device)
+    dst = torch.from_numpy(np.concatenate([e[:, 1], e[:, 0]])).to(device)
+    deg = torch.zeros(nvert, device=device).index_add_(0, src, torch.ones(src.numel(), device=device))
+    inv = (1.0 / deg.clamp(min=1.0))[:, None]
+
+    def lap(p: torch.Tensor) -> torch.Tensor:
+        return p - torch.zeros_like(p).index_add_(0, src, p[dst]) * inv
+
+    return lap
+

@@ -126,3 +126,26 @@ def test_context_every_tile_shape(ctx, shape):
             assert_same(gpu_render(ctx, [m], R, w, h, image, U=U), ref, f"shape {shape} {w}x{h}")
     finally:
         ctx.set_tile_shape(0)
+
+
+def test_batch_dense_frames_split_tiles(ctx):
+    """Frames whose tiles hold more than 8192 entries (rasterized in slices) next to
+    ordinary frames, planned and replayed."""
+    dense = W.soup(50000, seed=43, n_large=3)
+    ico = W.displaced_icosphere(3, seed=3)
+    meshes = {"dense": dense, "ico": ico}
+    dev = {k: dev_mesh(ctx, m) for k, m in meshes.items()}
+    frames = []
+    for i, (w, h, image, names) in enumerate([(80, 24, True, ["dense"]), (160, 48, False, ["ico"]),
+                                              (64, 32, True, ["dense", "ico"]), (33, 9, False, ["dense"])]):
+        R = O.euler_rotation(*W.cli_rotation(yaw=0.4 * i, pitch=0.2 * i))
+        U = O.viewport_transform(w, h, O.scene_extent([meshes[n]["bbox_max"] for n in names]))
+        frames.append({"w": w, "h": h, "image": image, "U": U, "names": names, "R": R,
+                       "draws": [(dev[n], R) for n in names]})
+    b = S.Batch(ctx, frames)
+    b.render()
+    check_frames(b, meshes, frames, "planned")
+    b.render()
+    b.render()
+    check_frames(b, meshes, frames, "graph")
+    b.close()

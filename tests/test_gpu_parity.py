@@ -124,10 +124,20 @@ def test_scaled_config2_soup(ctx, w, h):
     for image in (True, False):
         ref = oracle_render([m], R, w, h, image)
         assert_same(gpu_render(ctx, [m], R, w, h, image), ref, f"soup {w}x{h}")
-    # the depth culling is active here: it skips some of the covered samples
-    culled = gpu_render(ctx, [m], R, w, h, True, depth_cull=True)
+
+
+
+def test_depth_culling_skips_hidden_fragments(ctx):
+    """At config 2's triangle size and depth complexity (1/8 of its viewport: 1/64 of the
+    triangles, 8x the vertex offsets) the depth culling skips most covered samples and
+    leaves every buffer as it is."""
+    m = W.soup(16000, seed=5, n_large=4, sigma=0.16)
+    R = O.euler_rotation(*W.cli_rotation())
+    w, h = 480, 270
+    ref = oracle_render([m], R, w, h, True)
+    assert_same(gpu_render(ctx, [m], R, w, h, True, depth_cull=True), ref, "dense soup")
     ctx.set_depth_cull(True)
-    assert ctx.fragments() < ref.fragments
+    assert ctx.fragments() < 0.75 * ref.fragments
 
 
 def test_yawed_soup_wraps(ctx):
@@ -199,3 +209,15 @@ def test_draw_without_clear_errors(ctx):
     with pytest.raises(S.SlothError):
         S.Mesh(c, m["x"], m["y"], m["z"], m["rgb"], idx=np.array([[0, 1, 99]]))
     c.close()
+
+
+def test_dense_small_viewport_split_tiles(ctx):
+    """Tens of thousands of triangles over a few tiles: tiles with more than 8192 entries
+    are rasterized in slices by separate CTAs that fold their keys with a global atomicMin;
+    a second draw folds into the first draw's keys."""
+    a = W.soup(60000, seed=41, n_large=5)
+    b = W.soup(30000, seed=42, n_large=2)
+    R = O.euler_rotation(*W.cli_rotation(yaw=0.7))
+    for w, h, image in ((80, 24, True), (81, 23, False)):
+        ref = oracle_render([a, b], R, w, h, image)
+        assert_same(gpu_render(ctx, [a, b], R, w, h, image), ref, f"dense {w}x{h}")
