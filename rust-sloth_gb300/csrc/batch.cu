@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256) batch_items_kernel(BatchDev b)
 // or a slice of a split tile) of the item list built by batch_items_kernel; the hardware
 // block scheduler keeps the SMs fed as CTAs finish.  CTAs past the item count return.
 template <int TW, int TH>
-__global__ void __launch_bounds__(kRasterThreads) batch_raster_kernel(BatchDev b)
+__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) batch_raster_kernel(BatchDev b)
 {
     __shared__ TileSmem<TW, TH> S;
     if (b.bb.tile_offset[b.total_tiles] > b.bb.capacity) {

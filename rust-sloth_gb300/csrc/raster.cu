@@ -6,7 +6,7 @@ namespace sloth {
 
 // One CTA per raster item (tile, slice); CTAs past the item count return at once.
 template <int TW, int TH>
-__global__ void __launch_bounds__(kRasterThreads)
+__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks)
 raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb, uint32_t ntiles, int depth_cull)
 {
     __shared__ TileSmem<TW, TH> S;

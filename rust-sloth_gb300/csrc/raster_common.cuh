@@ -24,6 +24,7 @@ namespace sloth {
 
 constexpr int kSortCap = 2048;   // entries sorted per pass (16 KB of shared memory)
 constexpr int kRasterThreads = 256;
+constexpr int kRasterMinBlocks = 5;   // resident CTAs per SM the register budget allows
 
 template <int TW, int TH>
 struct TileSmem {
@@ -79,6 +80,57 @@ __device__ __forceinline__ void raster_part(const TriRecord &r, uint32_t gtri, R
     }
 }
 
+// ---- lane mode: one lane per entry (tiles of few entries, mostly small triangles) ----
+
+// The part of a record's samples (unwrapped or wrapped) that falls in tile (tr, tc),
+// clipped to the tile; empty when the exact corner test shows no covered sample.
+template <int kNotWrapped>
+__device__ __forceinline__ Rect tile_part(const TriRecord &r, const Viewport &vp, int tr, int tc)
+{
+    const Rect p = kNotWrapped ? unwrapped_part(vp, r.x0, r.xe, r.y0, r.y1) : wrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
+    if (p.empty()) return Rect{0, 0, 0, 0};
+    const Rect c = kNotWrapped ? clip_unwrapped(vp, p, tr, tc) : clip_wrapped(vp, p, tr, tc);
+    if (c.empty() || ((r.flags & kFlagFiniteXY) && !rect_may_cover(r, c))) return Rect{0, 0, 0, 0};
+    return c;
+}
+
+__device__ __forceinline__ int rect_area(const Rect &c)
+{
+    return c.empty() ? 0 : (c.xb - c.xa) * (c.yb - c.ya);
+}
+
+// One sample of the reference's loop body: edge test, depth, key folded into the tile.
+template <int TW, int kNotWrapped>
+__device__ __forceinline__ void fold_sample(const TriRecord &r, uint32_t gtri, int x, int y, int R0, int C0,
+                                            int w, unsigned long long *skeys, uint32_t &frags)
+{
+    const EdgeVals e = eval_edges(r, (float)x, (float)y);
+    if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
+        ++frags;
+        const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
+        if (z < kFltMax) {
+            const unsigned long long key = make_key(z, gtri, kNotWrapped);
+            const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
+            const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
+            unsigned long long *p = &skeys[row * TW + col];
+            if (key < *(volatile unsigned long long *)p) atomicMin(p, key);
+        }
+    }
+}
+
+// One lane walks every sample of rect c.
+template <int TW, int kNotWrapped>
+__device__ __forceinline__ void raster_serial(const TriRecord &r, uint32_t gtri, const Rect &c, int R0, int C0,
+                                              int w, unsigned long long *skeys, uint32_t &frags)
+{
+    for (int y = c.ya; y < c.yb; ++y)
+        for (int x = c.xa; x < c.xb; ++x) fold_sample<TW, kNotWrapped>(r, gtri, x, y, R0, C0, w, skeys, frags);
+}
+
+// Entries whose clipped rectangles hold at most this many samples are walked by their
+// lane alone; larger ones by the whole warp.
+constexpr int kSerialMaxSamples = 16;
+
 // Upper bounds of the farthest depth (ordered high key word) among the tile's cells that
 // unwrapped samples can write (row y in [1,h-2], column 2x in [2,w-1], even) and among
 // those wrapped samples can write (row y+1 in [2,h-1], column 2x-w in [0,w-4], of the
@@ -127,6 +179,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
     const int lane = threadIdx.x & 31;
     const Viewport vp{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
     uint32_t frags = 0;
+    const int wid = threadIdx.x >> 5;
     for (uint32_t base = 0; base < cnt; base += kSortCap) {
         const uint32_t n = min(cnt - base, (uint32_t)kSortCap);
         uint32_t np2 = 2;
@@ -151,38 +204,81 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                     block_sync();
                 }
         }
-        for (;;) {
-            uint32_t e = 0;
-            if (lane == 0) e = atomicAdd(&S.next, 1u);
-            e = __shfl_sync(0xffffffffu, e, 0);
-            if (e >= n) break;
-            const unsigned long long ent = S.ent[e];
-            if (depth_cull) {
-                if ((e & 15) == 15) {
-                    uint32_t mu, mw;
-                    tile_zmax<TW, TH>(S.keys, R0, C0, g, lane, mu, mw);
-                    if (lane == 0) {
-                        atomicMin(&S.zmax_u, mu);
-                        atomicMin(&S.zmax_w, mw);
-                    }
-                }
-                const uint32_t zlo = (uint32_t)(ent >> 32);
+        // Windows of kRasterThreads sorted entries; lane i of warp w takes entry w + 8i, so
+        // that the warps move through the sorted order together.  Each lane loads its own
+        // record; a small triangle is walked by its lane, a larger one by the whole warp
+        // (in the warp's sorted order, each checked against the depth bound right before
+        // it).
+        bool stop = false;        // warp-uniform: the rest of this warp's entries are hidden
+        // warp-uniform count of warp walks since the warp's last refresh of the bound: one
+        // refresh per 16 walks of a warp (about one per 16 entries of the CTA, as the
+        // warps take turns), warp w's first after 2 + 2w walks
+        uint32_t since = 14u - 2u * (uint32_t)wid;
+        for (uint32_t w0 = 0; w0 < n && !stop; w0 += kRasterThreads) {
+            const uint32_t e = w0 + wid + (kRasterThreads / 32) * lane;
+            const unsigned long long ent = e < n ? S.ent[e] : ~0ull;
+            bool live = e < n;
+            if (depth_cull && live) {
                 const uint32_t zu = *(volatile uint32_t *)&S.zmax_u, zw = *(volatile uint32_t *)&S.zmax_w;
-                const uint32_t lim = ((uint32_t)ent & 0x80000000u) ? max(zu, zw) : zu;
-                if (zlo > lim) {
-                    // sorted: every later entry is behind every writable cell too
-                    if (zlo > max(zu, zw)) break;
-                    continue;
-                }
+                if ((uint32_t)(ent >> 32) > (((uint32_t)ent & 0x80000000u) ? max(zu, zw) : zu)) live = false;
             }
             const uint32_t gtri = (uint32_t)ent & 0x7fffffffu;
-            const TriRecord r = load_record(fb.records, gtri);
-            const Rect U = unwrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
-            if (!U.empty())
-                raster_part<TW, 1>(r, gtri, clip_unwrapped(vp, U, tr, tc), R0, C0, g.w, S.keys, lane, frags);
-            const Rect W = wrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
-            if (!W.empty())
-                raster_part<TW, 0>(r, gtri, clip_wrapped(vp, W, tr, tc), R0, C0, g.w, S.keys, lane, frags);
+            // the sample range (x0, xe, y0, y1) alone sizes the tile's part of the triangle
+            int area = 0;
+            if (live) {
+                const int4 xr = __ldg(reinterpret_cast<const int4 *>(fb.records + gtri) + 4);
+                const Rect U = unwrapped_part(vp, xr.x, xr.y, xr.z, xr.w);
+                const Rect W = wrapped_part(vp, xr.x, xr.y, xr.z, xr.w);
+                if (!U.empty()) area += rect_area(clip_unwrapped(vp, U, tr, tc));
+                if (!W.empty()) area += rect_area(clip_wrapped(vp, W, tr, tc));
+            }
+            const bool serial = live && area <= kSerialMaxSamples;
+            if (serial) {
+                const TriRecord r = load_record(fb.records, gtri);
+                raster_serial<TW, 1>(r, gtri, tile_part<1>(r, vp, tr, tc), R0, C0, g.w, S.keys, frags);
+                raster_serial<TW, 0>(r, gtri, tile_part<0>(r, vp, tr, tc), R0, C0, g.w, S.keys, frags);
+            }
+            unsigned coop = __ballot_sync(0xffffffffu, live && !serial);
+            while (coop) {
+                const int src = __ffs(coop) - 1;
+                coop &= coop - 1;
+                if (depth_cull) {
+                    if (since >= 16) {
+                        uint32_t mu, mw;
+                        tile_zmax<TW, TH>(S.keys, R0, C0, g, lane, mu, mw);
+                        if (lane == 0) {
+                            atomicMin(&S.zmax_u, mu);
+                            atomicMin(&S.zmax_w, mw);
+                        }
+                        since = 0;
+                    }
+                    ++since;
+                    // lane 0 decides for the warp (the bounds may move between reads)
+                    const unsigned long long es = __shfl_sync(0xffffffffu, ent, src);
+                    uint32_t verdict = 0;
+                    if (lane == 0) {
+                        const uint32_t zlo = (uint32_t)(es >> 32);
+                        const uint32_t zu = *(volatile uint32_t *)&S.zmax_u, zw = *(volatile uint32_t *)&S.zmax_w;
+                        const uint32_t lim = ((uint32_t)es & 0x80000000u) ? max(zu, zw) : zu;
+                        verdict = zlo > max(zu, zw) ? 2u : (zlo > lim ? 1u : 0u);
+                    }
+                    verdict = __shfl_sync(0xffffffffu, verdict, 0);
+                    if (verdict == 2u) {
+                        // sorted: every later entry of this warp is behind every writable cell
+                        stop = true;
+                        break;
+                    }
+                    if (verdict == 1u) continue;
+                }
+                const uint32_t gt = __shfl_sync(0xffffffffu, gtri, src);
+                const TriRecord r = load_record(fb.records, gt);
+                const Rect U = unwrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
+                if (!U.empty())
+                    raster_part<TW, 1>(r, gt, clip_unwrapped(vp, U, tr, tc), R0, C0, g.w, S.keys, lane, frags);
+                const Rect W = wrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
+                if (!W.empty())
+                    raster_part<TW, 0>(r, gt, clip_wrapped(vp, W, tr, tc), R0, C0, g.w, S.keys, lane, frags);
+            }
         }
         block_sync();
     }
