@@ -150,8 +150,12 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_fill_kernel(BatchDev b
     TriRecord r;
     TileSpan sp{};
     if (live) {
-        r = f.fb.records[gtri];
-        sp = tile_span(vp, r);
+        // the sample range first: culled and off-screen triangles end here
+        const int4 xr = __ldg(reinterpret_cast<const int4 *>(f.fb.records + gtri) + 4);
+        if (xr.x < xr.y && xr.z < xr.w) {
+            r = f.fb.records[gtri];
+            sp = tile_span(vp, r);
+        }
     }
     fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, b.bb.tile_cursor + f.tile_off,
                     b.bb.entries, b.bb.capacity);
@@ -225,8 +229,12 @@ __global__ void __launch_bounds__(256) batch_resolve_kernel(BatchDev b, const in
     const BatchFrame &f = b.frames[blk.x];
     const uint64_t nz = (uint64_t)f.g.w * f.g.h;
     const uint64_t ncells = f.g.image ? nz + f.g.h : nz;
-    const uint64_t end = min(ncells, (uint64_t)blk.y + kBatchResolveChunk);
-    for (uint64_t c = (uint64_t)blk.y + threadIdx.x; c < end; c += blockDim.x) resolve_cell(f.g, f.fb, c);
+    const uint64_t end = min(ncells, (uint64_t)blk.y + kBatchResolveChunk);   // chunks start even
+    const int lane = threadIdx.x & 31;
+    for (uint32_t i = threadIdx.x; i < kBatchResolveChunk / 2; i += blockDim.x) {
+        const uint64_t p = (uint64_t)blk.y / 2 + i;
+        resolve_pair(f.g, f.fb, p, 2 * p < end, lane);
+    }
 }
 
 cudaError_t prepare_batch_kernels()

@@ -199,8 +199,12 @@ bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, 
     TriRecord r;
     TileSpan sp{};
     if (live) {
-        r = fb.records[gtri];
-        sp = tile_span(vp, r);
+        // the sample range first: culled and off-screen triangles end here
+        const int4 xr = __ldg(reinterpret_cast<const int4 *>(fb.records + gtri) + 4);
+        if (xr.x < xr.y && xr.z < xr.w) {
+            r = fb.records[gtri];
+            sp = tile_span(vp, r);
+        }
     }
     fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
 }

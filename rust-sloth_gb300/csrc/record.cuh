@@ -107,6 +107,13 @@ __device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p
     r.xe = x1;
     r.zlo = -INFINITY;
     if (finite && r.x0 < x1 && r.y0 < r.y1) {
+        // back faces first: the bounds over the untightened range hold over any subrange,
+        // so a triangle proven empty here needs no tighter range
+        if (provably_empty(orient_bound(r))) {
+            r.xe = r.x0;
+            r.flags |= kFlagCulled;
+            return r;
+        }
         // first column strictly right of the triangle, not left of x0
         const float xf = fadd(floorf(mxx), 1.0f);
         if (xf < (float)x1) {

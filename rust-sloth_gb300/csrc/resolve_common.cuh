@@ -33,7 +33,8 @@ __device__ __forceinline__ bool later(const Cand &a, const Cand &b)
 
 __device__ __forceinline__ uint64_t key_at(const FrameGeom &g, const FrameBuffers &fb, int r, int cc)
 {
-    const int tile = (r / g.th) * g.ntx + cc / g.tw;
+    // tile sides are powers of two
+    const int tile = (r >> (__ffs(g.th) - 1)) * g.ntx + (cc >> (__ffs(g.tw) - 1));
     if (fb.tile_gen[tile] != fb.gen) return kEmptyKey;
     return fb.keys[(size_t)r * g.pitch + cc];
 }
@@ -107,6 +108,130 @@ __device__ __forceinline__ void resolve_cell(const FrameGeom &g, const FrameBuff
         }
     }
     fb.cells_out[c] = best.cell;
+}
+
+// The newline candidate of frame cell c (r, cc its row and column when c < w*h), if the
+// frame is in image mode and c = y*w+1 for a row y some triangle spans.
+__device__ __forceinline__ bool newline_at(const FrameGeom &g, const FrameBuffers &fb, uint64_t c, uint64_t nz, int r,
+                                          int cc, Cand &out)
+{
+    if (!g.image || c == 0) return false;
+    uint64_t yn;
+    if (c < nz && g.w > 1) {
+        if (cc != 1) return false;
+        yn = (uint64_t)r;
+    } else {
+        if ((c - 1) % (uint64_t)g.w != 0) return false;
+        yn = (c - 1) / (uint64_t)g.w;
+        if (yn >= (uint64_t)g.h) return false;
+    }
+    const int32_t t = nltree_query(fb.nltree, g.nl_size, (int)yn);
+    if (t < 0) return false;
+    out = Cand{(uint32_t)t, (int32_t)yn, INT_MAX, (uint32_t)'\n'};
+    return true;
+}
+
+__device__ __forceinline__ Cand shfl_up_cand(const Cand &c)
+{
+    return Cand{__shfl_up_sync(0xffffffffu, c.tri, 1), __shfl_up_sync(0xffffffffu, c.y, 1),
+                __shfl_up_sync(0xffffffffu, c.x, 1), __shfl_up_sync(0xffffffffu, c.cell, 1)};
+}
+
+// Resolve frame cells c0 = 2p and c0+1, and depth cells c0 and c0+1, of one frame (the
+// rule of resolve_cell).  Called by all 32 lanes of a warp with consecutive p in lane
+// order; lanes with valid false (past the end) write nothing.  Depth cell c0-1's winner
+// is the previous lane's second depth cell (lane 0 decodes it itself), so a pair costs
+// two key reads and two record decodes.
+__device__ __forceinline__ void resolve_pair(const FrameGeom &g, const FrameBuffers &fb, uint64_t p, bool valid,
+                                             int lane)
+{
+    const uint64_t nz = (uint64_t)g.w * g.h;
+    const uint64_t ncells = g.image ? nz + g.h : nz;
+    const uint64_t c0 = 2 * p;
+    int r0 = 0, cc0 = 0;
+    if (valid && c0 < nz) {
+        if (nz <= 0xffffffffull) {
+            r0 = (int)((uint32_t)c0 / (uint32_t)g.w);
+        } else {
+            r0 = (int)(c0 / (uint64_t)g.w);
+        }
+        cc0 = (int)(c0 - (uint64_t)r0 * g.w);
+    }
+    int r1 = r0, cc1 = cc0 + 1;
+    if (cc1 == g.w) {
+        ++r1;
+        cc1 = 0;
+    }
+    Cand k0{0, 0, 0, (uint32_t)' '}, k1{0, 0, 0, (uint32_t)' '};
+    bool h0 = false, h1 = false;
+    float z0 = kFltMax, z1 = kFltMax;
+    if (valid && c0 < nz) {
+        const uint64_t k = key_at(g, fb, r0, cc0);
+        if (k != kEmptyKey) {
+            k0 = decode(g, fb, k, r0, cc0, &z0);
+            h0 = true;
+        }
+    }
+    if (valid && c0 + 1 < nz) {
+        const uint64_t k = key_at(g, fb, r1, cc1);
+        if (k != kEmptyKey) {
+            k1 = decode(g, fb, k, r1, cc1, &z1);
+            h1 = true;
+        }
+    }
+    // depth cell c0-1
+    Cand km = shfl_up_cand(k1);
+    bool hm = __shfl_up_sync(0xffffffffu, (int)h1, 1) != 0;
+    if (lane == 0) {
+        hm = false;
+        if (valid && c0 >= 1 && c0 - 1 < nz) {
+            int rm, cm;
+            if (c0 < nz) {
+                rm = cc0 > 0 ? r0 : r0 - 1;
+                cm = cc0 > 0 ? cc0 - 1 : g.w - 1;
+            } else {
+                rm = g.h - 1;
+                cm = g.w - 1;
+            }
+            const uint64_t k = key_at(g, fb, rm, cm);
+            if (k != kEmptyKey) {
+                km = decode(g, fb, k, rm, cm, nullptr);
+                hm = true;
+            }
+        }
+    }
+    if (!valid) return;
+    // frame cell c0: depth cells c0 and c0-1, newline; frame cell c0+1: c0+1 and c0
+    if (c0 < ncells) {
+        bool have = h0;
+        Cand best = k0;
+        if (hm && (!have || later(km, best))) {
+            best = km;
+            have = true;
+        }
+        Cand n;
+        if (newline_at(g, fb, c0, nz, r0, cc0, n) && (!have || later(n, best))) best = n;
+        fb.cells_out[c0] = best.cell;
+    }
+    if (c0 + 1 < ncells) {
+        bool have = h1;
+        Cand best = k1;
+        if (h0 && (!have || later(k0, best))) {
+            best = k0;
+            have = true;
+        }
+        Cand n;
+        if (newline_at(g, fb, c0 + 1, nz, r1, cc1, n) && (!have || later(n, best))) best = n;
+        fb.cells_out[c0 + 1] = best.cell;
+    }
+    if (c0 < nz) {
+        fb.z_out[c0] = z0;
+        fb.winner_out[c0] = h0 ? (int32_t)k0.tri : -1;
+    }
+    if (c0 + 1 < nz) {
+        fb.z_out[c0 + 1] = z1;
+        fb.winner_out[c0 + 1] = h1 ? (int32_t)k1.tri : -1;
+    }
 }
 
 }  // namespace sloth
