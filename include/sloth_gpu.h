@@ -125,6 +125,25 @@ sloth_status sloth_ctx_device_buffers(sloth_ctx *ctx, const uint32_t **cells, co
  * sample when SLOTH_OPTION_DEPTH_CULL is 0.  Blocks until pending work completes. */
 sloth_status sloth_ctx_fragments(sloth_ctx *ctx, uint64_t *fragments);
 
+/* The bytes Context::flush(color, webify) prints for the frame (src/context.rs:50-92),
+ * formatted on the GPU from the resolved frame cells:
+ *   SLOTH_FLUSH_PLAIN  color false: every char, then "\n" (println);
+ *   SLOTH_FLUSH_ANSI   color true, webify false: per cell crossterm's styled char,
+ *                      ESC[48;2;25;25;25m ESC[38;2;<r>;<g>;<b>m <char> ESC[0m;
+ *   SLOTH_FLUSH_HTML   color true, webify true: per cell <span style="color:rgb(<r>,<g>,<b>)"><char>.
+ * A terminal context (image 0) starts with crossterm's MoveTo(0,0), ESC[1;1H.  The ANSI
+ * form restates crossterm 0.18.0 (the version the reference's Cargo.lock pins), whose
+ * source is not part of the reference.
+ * sloth_ctx_flush: *bytes = the size; with out != NULL the bytes are copied there
+ * (SLOTH_ERR_LIMIT if capacity < size).  Blocks.
+ * sloth_ctx_flush_device: the bytes stay on the device (valid until the next flush of the
+ * context or its destruction). */
+#define SLOTH_FLUSH_PLAIN 0
+#define SLOTH_FLUSH_ANSI 1
+#define SLOTH_FLUSH_HTML 2
+sloth_status sloth_ctx_flush(sloth_ctx *ctx, int format, char *out, uint64_t capacity, uint64_t *bytes);
+sloth_status sloth_ctx_flush_device(sloth_ctx *ctx, int format, const char **device_bytes, uint64_t *bytes);
+
 /* Options (sloth_ctx_set_option).
  * SLOTH_OPTION_DEPTH_CULL: 1 (default) lets the raster skip triangles proven to lie
  *   behind every depth cell they could write (a proven depth bound against the tile's
@@ -210,6 +229,9 @@ sloth_status sloth_batch_frame_buffers(sloth_batch *batch, uint32_t frame, const
 /* Fragments the raster evaluated in the last render, summed over frames (see
  * sloth_ctx_fragments); blocks. */
 sloth_status sloth_batch_fragments(sloth_batch *batch, uint64_t *fragments);
+/* sloth_ctx_flush for one frame of the batch. */
+sloth_status sloth_batch_flush(sloth_batch *batch, uint32_t frame, int format, char *out, uint64_t capacity,
+                               uint64_t *bytes);
 /* Use tile shape `shape` (sloth_tile_shape) for this batch; re-lays out its buffers. */
 sloth_status sloth_batch_set_tile_shape(sloth_batch *batch, int shape);
 /* Autotuner: render the batch `reps` times with every tile shape, keep the fastest;

@@ -53,6 +53,8 @@ def lib() -> C.CDLL:
         L.orc_draw_mesh.argtypes = [C.POINTER(OrcCtx), f32p, f32p, f32p, u32p, u8p, C.c_uint32, f32p]
         L.orc_draw_mesh_banded.argtypes = [C.POINTER(OrcCtx), f32p, f32p, f32p, u32p, u8p, C.c_uint32,
                                            f32p, C.c_int]
+        L.orc_flush.restype = C.c_uint64
+        L.orc_flush.argtypes = [u32p, C.c_uint64, C.c_int, C.c_int, C.c_char_p]
         _lib = L
     return _lib
 
@@ -120,6 +122,18 @@ def triangle_normal(v12) -> np.ndarray:
 
 def default_shader(s: float) -> str:
     return lib().orc_default_shader(C.c_float(s)).decode()
+
+
+FLUSH_PLAIN, FLUSH_ANSI, FLUSH_HTML = 0, 1, 2
+
+
+def flush(cells, image: bool, fmt: int) -> bytes:
+    """Context::flush's stdout bytes for a frame of cells (src/context.rs:50-92)."""
+    c = np.ascontiguousarray(cells, np.uint32)
+    n = int(lib().orc_flush(_p(c, C.c_uint32), c.size, 1 if image else 0, fmt, None))
+    buf = C.create_string_buffer(n)
+    lib().orc_flush(_p(c, C.c_uint32), c.size, 1 if image else 0, fmt, buf)
+    return buf.raw[:n]
 
 
 @dataclass

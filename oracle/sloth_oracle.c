@@ -26,6 +26,7 @@
 
 #include <math.h>
 #include <pthread.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -405,3 +406,35 @@ void orc_draw_mesh_banded(orc_ctx *ctx, const float *x, const float *y, const fl
     free(jobs);
     free(setups);
 }
+
+/* ---------------- Context::flush (src/context.rs:50-92) ---------------- */
+
+static uint64_t put_bytes(char *out, uint64_t at, const char *s, uint64_t n)
+{
+    if (out) memcpy(out + at, s, n);
+    return n;
+}
+
+uint64_t orc_flush(const uint32_t *cells, uint64_t ncells, int image, int format, char *out)
+{
+    uint64_t n = 0;
+    char buf[64];
+    if (!image) n += put_bytes(out, n, "\x1b[1;1H", 6);          /* stdout.queue(cursor::MoveTo(0, 0)) */
+    for (uint64_t i = 0; i < ncells; ++i) {
+        const unsigned ch = cells[i] & 255u, r = (cells[i] >> 8) & 255u, g = (cells[i] >> 16) & 255u,
+                       b = cells[i] >> 24;
+        int k;
+        if (format == 0) {
+            buf[0] = (char)ch;
+            k = 1;
+        } else if (format == 1) {
+            k = snprintf(buf, sizeof buf, "\x1b[48;2;25;25;25m\x1b[38;2;%u;%u;%um%c\x1b[0m", r, g, b, (char)ch);
+        } else {
+            k = snprintf(buf, sizeof buf, "<span style=\"color:rgb(%u,%u,%u)\">%c", r, g, b, (char)ch);
+        }
+        n += put_bytes(out, n, buf, (uint64_t)k);
+    }
+    if (format == 0) n += put_bytes(out, n, "\n", 1);            /* println!("{}", frame) */
+    return n;
+}
+

@@ -99,4 +99,12 @@ void orc_draw_mesh_banded(orc_ctx *ctx, const float *x, const float *y, const fl
 #ifdef __cplusplus
 }
 #endif
+/* src/context.rs:50-92 Context::flush(color, webify): the bytes written to stdout for a
+ * frame of cells (char | r<<8 | g<<16 | b<<24).  format 0: color false (chars, then
+ * println's newline); 1: color true, webify false (per cell crossterm 0.18's styled char:
+ * ESC[48;2;25;25;25m ESC[38;2;r;g;bm char ESC[0m); 2: color true, webify true (per cell
+ * <span style="color:rgb(r,g,b)">char).  A terminal context (image 0) starts with
+ * crossterm's MoveTo(0,0) = ESC[1;1H.  out may be NULL (size only); returns the size. */
+uint64_t orc_flush(const uint32_t *cells, uint64_t ncells, int image, int format, char *out);
+
 #endif

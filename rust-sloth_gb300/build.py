@@ -19,7 +19,7 @@ OUT_DIR = HERE / "_build"
 LIB = OUT_DIR / "libsloth_gpu.so"
 
 SOURCES = ["setup.cu", "bin.cu", "raster.cu", "resolve.cu", "sloth_api.cu", "noalloc.cu", "batch.cu",
-           "batch_api.cu", "diff.cu"]
+           "batch_api.cu", "diff.cu", "flush.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-ftz=false",
@@ -73,5 +73,37 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
+HOST = HERE / "host"
+HOST_SOURCES = ["loaders.cpp", "context.cpp", "main.cpp"]
+CLI = OUT_DIR / "sloth"
+MESHDUMP = OUT_DIR / "sloth_meshdump"
+HOST_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-I", str(INCLUDE)]
+
+
+def build_host(force: bool = False, verbose: bool = False) -> Path:
+    """Compile the C++ host side (loaders, Context mirror, the `sloth` command) against
+    libsloth_gpu.so; returns the command's path."""
+    lib = build_library(force=force, verbose=verbose)
+    deps = [HOST / s for s in HOST_SOURCES] + [HOST / "sloth_host.hpp", INCLUDE / "sloth_gpu.h", lib, Path(__file__)]
+    jobs = []
+    if force or _stale(CLI, deps):
+        jobs.append(["g++"] + HOST_FLAGS + [str(HOST / s) for s in HOST_SOURCES] + [
+            "-o", str(CLI), "-L", str(OUT_DIR), "-lsloth_gpu", "-Wl,-rpath,$ORIGIN"])
+    dump_deps = [HOST / "meshdump.cpp", HOST / "loaders.cpp", HOST / "sloth_host.hpp", Path(__file__)]
+    if force or _stale(MESHDUMP, dump_deps):
+        # the loaders alone, no GPU library: usable where there is no CUDA device
+        jobs.append(["g++"] + HOST_FLAGS + [str(HOST / "meshdump.cpp"), str(HOST / "loaders.cpp"),
+                                            "-o", str(MESHDUMP)])
+    procs = [subprocess.Popen(c, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True) for c in jobs]
+    for c, p in zip(jobs, procs):
+        out, err = p.communicate()
+        if verbose:
+            print(" ".join(c))
+        if p.returncode != 0:
+            raise RuntimeError(f"host build failed:\n{out}\n{err}")
+    return CLI
+
+
 if __name__ == "__main__":
     print(build_library(force=True, verbose=True))
+    print(build_host(verbose=True))

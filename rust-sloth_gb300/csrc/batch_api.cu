@@ -14,6 +14,7 @@
 
 #include "batch_kernels.h"
 #include "diff_kernels.h"
+#include "flush_kernels.h"
 #include "sloth_gpu.h"
 #include "sloth_internal.cuh"
 
@@ -67,6 +68,8 @@ struct sloth_batch {
     uint32_t ndiff_blk = 0;
     uint2 *vis = nullptr;                     // stored visibility, one per depth cell
     bool vis_valid = false;                   // vis holds the last render's visibility
+
+    FlushScratch flush;
 };
 
 // Shared with sloth_api.cu.
@@ -478,6 +481,7 @@ void sloth_batch_destroy(sloth_batch *b)
     free_layout(b);
     bfree(b->diff_blk);
     bfree(b->vis);
+    flush_release(b->flush);
     if (b->h_mats) cudaFreeHost(b->h_mats);
     if (b->h_total) cudaFreeHost(b->h_total);
     if (b->h_overflow) cudaFreeHost(b->h_overflow);
@@ -525,6 +529,26 @@ sloth_status sloth_batch_read(sloth_batch *b, uint32_t frame, uint32_t *cells, f
     if (z) BCU(b, cudaMemcpyAsync(z, b->z + b->z_off[frame], nz * 4, cudaMemcpyDeviceToHost, b->stream));
     if (winner)
         BCU(b, cudaMemcpyAsync(winner, b->winner + b->z_off[frame], nz * 4, cudaMemcpyDeviceToHost, b->stream));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    return SLOTH_OK;
+}
+
+sloth_status sloth_batch_flush(sloth_batch *b, uint32_t frame, int format, char *out, uint64_t capacity,
+                               uint64_t *bytes)
+{
+    if (!b || frame >= b->frames.size() || !bytes) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (format < SLOTH_FLUSH_PLAIN || format > SLOTH_FLUSH_HTML)
+        return sloth_ctx_fail(b->ctx, SLOTH_ERR_INVALID_ARGUMENT, "unknown flush format");
+    if (!b->rendered) return sloth_ctx_fail(b->ctx, SLOTH_ERR_INVALID_ARGUMENT, "render the batch first");
+    BCU(b, cudaSetDevice(b->device));
+    sloth_status st = settle(b);
+    if (st != SLOTH_OK) return st;
+    const uint64_t nc = b->cell_off[frame + 1] - b->cell_off[frame];
+    BCU(b, flush_run(b->flush, b->cells + b->cell_off[frame], nc, b->frames[frame].image ? 1 : 0, format, b->stream,
+                     bytes));
+    if (!out) return SLOTH_OK;
+    if (capacity < *bytes) return sloth_ctx_fail(b->ctx, SLOTH_ERR_LIMIT, "flush output buffer too small");
+    BCU(b, cudaMemcpyAsync(out, b->flush.out, *bytes, cudaMemcpyDeviceToHost, b->stream));
     BCU(b, cudaStreamSynchronize(b->stream));
     return SLOTH_OK;
 }

@@ -19,6 +19,7 @@
 
 #include "sloth_internal.cuh"
 #include "sloth_kernels.h"
+#include "flush_kernels.h"
 
 using namespace sloth;
 
@@ -77,6 +78,8 @@ struct sloth_ctx {
     bool timing = false;
     std::map<std::string, KernelClock> clocks;
     uint64_t launches = 0;
+
+    FlushScratch flush;
 };
 
 // ---------------------------------------------------------------------------------------
@@ -385,6 +388,7 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     dfree(ctx->tv);
     if (ctx->h_total) cudaFreeHost(ctx->h_total);
     if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
+    flush_release(ctx->flush);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -473,6 +477,43 @@ sloth_status sloth_ctx_read(sloth_ctx *ctx, uint32_t *cells, float *z, int32_t *
         CU(ctx, cudaMemcpyAsync(winner, ctx->fb.winner_out, nz * sizeof(int32_t),
                                 cudaMemcpyDeviceToHost, ctx->stream));
     CU(ctx, cudaStreamSynchronize(ctx->stream));
+    return SLOTH_OK;
+}
+
+static sloth_status ctx_flush(sloth_ctx *ctx, int format, uint64_t *bytes)
+{
+    if (format < SLOTH_FLUSH_PLAIN || format > SLOTH_FLUSH_HTML)
+        return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "unknown flush format %d", format);
+    CU(ctx, cudaSetDevice(ctx->device));
+    sloth_status st = resolve_pending(ctx);
+    if (st != SLOTH_OK) return st;
+    const uint64_t nz = (uint64_t)ctx->g.w * ctx->g.h;
+    const uint64_t ncells = ctx->g.image ? nz + ctx->g.h : nz;
+    CU(ctx, timed(ctx, "flush", [&] {
+        return flush_run(ctx->flush, ctx->fb.cells_out, ncells, ctx->g.image, format, ctx->stream, bytes);
+    }));
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_flush(sloth_ctx *ctx, int format, char *out, uint64_t capacity, uint64_t *bytes)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!bytes) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "bytes is NULL");
+    sloth_status st = ctx_flush(ctx, format, bytes);
+    if (st != SLOTH_OK || !out) return st;
+    if (capacity < *bytes) return fail(ctx, SLOTH_ERR_LIMIT, "flush needs %llu bytes", (unsigned long long)*bytes);
+    CU(ctx, cudaMemcpyAsync(out, ctx->flush.out, *bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(ctx, cudaStreamSynchronize(ctx->stream));
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_flush_device(sloth_ctx *ctx, int format, const char **device_bytes, uint64_t *bytes)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!bytes || !device_bytes) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "bytes/device_bytes is NULL");
+    sloth_status st = ctx_flush(ctx, format, bytes);
+    if (st != SLOTH_OK) return st;
+    *device_bytes = ctx->flush.out;
     return SLOTH_OK;
 }
 

@@ -20,6 +20,7 @@ HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libsloth_gpu.so"
 
 OK = 0
+ERR_INVALID_ARGUMENT, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_LIMIT, ERR_DEVICE_FAULT = 1, 2, 3, 4, 5
 OPTION_DEPTH_CULL = 1
 OPTION_TILE_SHAPE = 2
 STATUS ={0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "LIMIT", 5: "DEVICE_FAULT"}
@@ -70,6 +71,9 @@ SIGNATURES = {
     "sloth_batch_set_tile_shape": (C.c_int, [_vp, C.c_int]),
     "sloth_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "sloth_batch_depth_cells": (C.c_int, [_vp, C.c_uint32, _u64p, _u64p]),
+    "sloth_ctx_flush": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_uint64, _u64p]),
+    "sloth_ctx_flush_device": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_void_p), _u64p]),
+    "sloth_batch_flush": (C.c_int, [_vp, C.c_uint32, C.c_int, C.c_char_p, C.c_uint64, _u64p]),
     "sloth_batch_shade": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int]),
     "sloth_batch_shade_backward": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sloth_ctx_set_timing": (C.c_int, [_vp, C.c_int]),
@@ -164,6 +168,11 @@ class Context:
         if st != OK:
             raise SlothError(st, self.lib.sloth_ctx_last_error(self.h).decode())
 
+    def flush(self, fmt: int = 1) -> bytes:
+        """Context::flush's stdout bytes for the current frame (FLUSH_PLAIN / _ANSI / _HTML),
+        formatted on the GPU."""
+        return _flush_bytes(lambda out, cap, n: self._check(self.lib.sloth_ctx_flush(self.h, fmt, out, cap, n)))
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.sloth_ctx_destroy(self.h)
@@ -244,6 +253,17 @@ class Context:
 
     def launch_count(self) -> int:
         return int(self.lib.sloth_ctx_launch_count(self.h))
+
+
+FLUSH_PLAIN, FLUSH_ANSI, FLUSH_HTML = 0, 1, 2
+
+
+def _flush_bytes(call) -> bytes:
+    n = C.c_uint64()
+    call(None, 0, C.byref(n))
+    buf = C.create_string_buffer(max(1, n.value))
+    call(buf, n.value, C.byref(n))
+    return buf.raw[:n.value]
 
 
 class Mesh:
@@ -389,6 +409,11 @@ class Batch:
         s, ms = C.c_int(), C.c_float()
         self.ctx._check(self.lib.sloth_batch_autotune(self.h, reps, C.byref(s), C.byref(ms)))
         return s.value, ms.value
+
+    def flush(self, frame: int, fmt: int = 1) -> bytes:
+        """Context::flush's stdout bytes for one frame, formatted on the GPU."""
+        return _flush_bytes(lambda out, cap, n: self.ctx._check(
+            self.lib.sloth_batch_flush(self.h, frame, fmt, out, cap, n)))
 
     # ---- differentiable shading (device pointers as ints, e.g. torch data_ptr()) ----
     def depth_cells(self, frame: int) -> tuple[int, int]:

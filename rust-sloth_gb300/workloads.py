@@ -189,27 +189,56 @@ def write_obj(path: Path | str, m: dict) -> None:
         fh.writelines(f"f {a + 1} {b + 1} {c + 1}\n" for a, b, c in idx.tolist())
 
 
+class LoadError(Exception):
+    """A file the reference's loaders would reject."""
+
+
+_libc = None
+
+
+def _strtof(tok: str) -> float:
+    """C strtof: the correctly rounded float32 of a decimal (Rust's f32::from_str), without
+    the double rounding of float() followed by a float32 cast."""
+    global _libc
+    import ctypes
+    try:
+        float(tok)
+    except ValueError:
+        raise LoadError(f"bad number {tok!r}")
+    if _libc is None:
+        _libc = ctypes.CDLL(None)
+        _libc.strtof.restype = ctypes.c_float
+        _libc.strtof.argtypes = [ctypes.c_char_p, ctypes.c_void_p]
+    return _libc.strtof(tok.encode(), None)
+
+
+def _rest(line: str, tag: str) -> str:
+    return line.split(tag, 1)[1].strip() if tag in line else ""
+
+
 def read_obj(path: Path | str) -> list[dict]:
-    """Read an OBJ the way the reference's loader sees it (tobj::load_obj with
-    GPU_LOAD_OPTIONS, then to_simple_mesh_with_materials, src/geometry.rs:83-148):
-    one mesh per object/group/material run, polygons fan-triangulated (v0,vi,vi+1),
-    colour = material Kd*255 truncated to u8, overridden by the first vertex's colour when
-    the file has vertex colours, (1,1,1) when there is no material library.
-    Restates tobj's published behaviour for the features the reference models use;
-    parity with tobj itself is not pinned."""
+    """Read an OBJ the way the reference's loader sees it (tobj 3.2.2 load_obj with
+    GPU_LOAD_OPTIONS, then to_simple_mesh_with_materials, src/geometry.rs:83-148): a new
+    mesh at every object or group, and at a change to a different known material; polygons
+    fan-triangulated (v0, vi, vi+1); colour = material Kd*255 as u8, replaced by the first
+    corner's vertex colour when `v` lines carry colours, (1,1,1) when the file has no
+    materials.  A missing material library or a face without a material when there are
+    materials are errors, as they are for the reference.  Restates tobj's published
+    behaviour for the features the reference models use; parity with tobj itself is not
+    pinned.  Every mesh is an unindexed soup with its origin-grown bounding box."""
     path = Path(path)
     pos, vcol = [], []
-    materials: dict[str, tuple] = {}
-    have_mtllib = False
-    groups = []   # (material name, [faces])
-    cur_faces: list = []
+    materials: list[tuple[str, list]] = []
+    mtl_failed = False
+    groups = []   # (material index or None, [corner position indices])
+    cur: list = []
     cur_mat = None
 
     def flush():
-        nonlocal cur_faces
-        if cur_faces:
-            groups.append((cur_mat, cur_faces))
-        cur_faces = []
+        nonlocal cur
+        if cur:
+            groups.append((cur_mat, cur))
+        cur = []
 
     for line in path.read_text(errors="replace").splitlines():
         parts = line.split()
@@ -217,49 +246,68 @@ def read_obj(path: Path | str) -> list[dict]:
             continue
         tag = parts[0]
         if tag == "v":
-            pos.append([float(t) for t in parts[1:4]])
+            if len(parts) < 4:
+                raise LoadError("PositionParseError")
+            pos.append([_strtof(t) for t in parts[1:4]])
             if len(parts) >= 7:
-                vcol.append([float(t) for t in parts[4:7]])
+                vcol.append([_strtof(t) for t in parts[4:7]])
         elif tag == "f":
             ids = []
             for tok in parts[1:]:
-                i = int(tok.split("/")[0])
-                ids.append(i - 1 if i > 0 else len(pos) + i)
+                head = tok.split("/")[0]
+                try:
+                    i = int(head)
+                except ValueError:
+                    raise LoadError("FaceParseError")
+                if i == 0:
+                    raise LoadError("FaceParseError")
+                j = i - 1 if i > 0 else len(pos) + i
+                if not 0 <= j < len(pos):
+                    raise LoadError("FaceVertexOutOfBounds")
+                ids.append(j)
             for k in range(1, len(ids) - 1):
-                cur_faces.append((ids[0], ids[k], ids[k + 1]))
+                cur += [ids[0], ids[k], ids[k + 1]]
         elif tag in ("o", "g"):
             flush()
         elif tag == "usemtl":
-            flush()
-            cur_mat = parts[1] if len(parts) > 1 else None
-        elif tag == "mtllib":
-            have_mtllib = True
-            mp = path.parent / " ".join(parts[1:])
-            if mp.exists():
-                name = None
-                for ml in mp.read_text(errors="replace").splitlines():
-                    mt = ml.split()
-                    if not mt:
-                        continue
-                    if mt[0] == "newmtl":
-                        name = " ".join(mt[1:])
-                        materials.setdefault(name, (0.0, 0.0, 0.0))
-                    elif mt[0] == "Kd" and name is not None:
-                        materials[name] = tuple(float(t) for t in mt[1:4])
+            name = _rest(line, "usemtl")
+            if not name:
+                raise LoadError("MaterialParseError")
+            found = next((k for k, (n, _) in enumerate(materials) if n == name), None)
+            if found is not None and found != cur_mat:
+                flush()
+            cur_mat = found
+        elif tag == "mtllib" and len(parts) > 1:
+            mp = path.parent / parts[1]
+            if not mp.exists():
+                mtl_failed = True
+                continue
+            for ml in mp.read_text(errors="replace").splitlines():
+                mt = ml.split()
+                if not mt or mt[0].startswith("#"):
+                    continue
+                if mt[0] == "newmtl":
+                    materials.append((_rest(ml, "newmtl"), [0.0, 0.0, 0.0]))
+                elif mt[0] == "Kd" and materials and len(mt) >= 4:
+                    materials[-1] = (materials[-1][0], [_strtof(t) for t in mt[1:4]])
     flush()
+    if mtl_failed:
+        raise LoadError("Expected to have materials.")
     P = np.array(pos, np.float32).reshape(-1, 3)
-    VC = np.array(vcol, np.float32).reshape(-1, 3) if len(vcol) == len(pos) and vcol else None
+    VC = np.array(vcol, np.float32).reshape(-1, 3)
     meshes = []
-    for mat, faces in groups:
-        F = np.array(faces, np.int64)
-        tri = P[F]
+    for mat, corners in groups:
+        F = np.array(corners, np.int64).reshape(-1, 3)
         col = np.ones((F.shape[0], 3), np.uint8)
-        if have_mtllib and materials:
-            kd = np.array(materials.get(mat, (0.0, 0.0, 0.0)), np.float32)
-            col[:] = _f32_to_u8(kd * np.float32(255.0))
-            if VC is not None:
+        if materials:
+            if mat is None:
+                raise LoadError("a face without a material")
+            col[:] = _f32_to_u8(np.array(materials[mat][1], np.float32) * np.float32(255.0))
+            if VC.size:
+                if F[:, 0].max() >= VC.shape[0]:
+                    raise LoadError("vertex colour index out of range")
                 col = _f32_to_u8(VC[F[:, 0]] * np.float32(255.0))
-        flat = tri.reshape(-1, 3)
+        flat = P[F].reshape(-1, 3)
         meshes.append(_mesh(flat[:, 0], flat[:, 1], flat[:, 2], None, col))
     return meshes
 
@@ -272,20 +320,25 @@ def _f32_to_u8(a: np.ndarray) -> np.ndarray:
 
 def read_stl(path: Path | str) -> dict:
     """Binary or ASCII STL, the way the reference sees it (stl_io 0.4.2 read_stl then
-    to_simple_mesh, src/geometry.rs:150-189): facets in file order, colour (255,255,0),
-    bounding box grown from (+MAX, -MAX) over the facets."""
+    to_simple_mesh, src/geometry.rs:150-189): ASCII when the file starts with "solid ",
+    binary otherwise; facets in file order, colour (255,255,0), bounding box grown from
+    (+MAX, -MAX) over the facets."""
     data = Path(path).read_bytes()
-    tris = None
-    if len(data) >= 84:
-        n = int.from_bytes(data[80:84], "little")
-        if 84 + 50 * n == len(data):
-            rec = np.frombuffer(data, dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("a", "<u2")]),
-                                count=n, offset=84)
-            tris = rec["v"].astype(np.float32)
-    if tris is None:
-        verts = [[float(t) for t in line.split()[1:4]] for line in data.decode(errors="replace").splitlines()
-                 if line.strip().startswith("vertex")]
+    if data.startswith(b"solid "):
+        verts = [[_strtof(t) for t in line.split()[1:4]] for line in data.decode(errors="replace").splitlines()
+                 if line.split()[:1] == ["vertex"]]
+        if len(verts) % 3:
+            raise LoadError("incomplete facet")
         tris = np.array(verts, np.float32).reshape(-1, 3, 3)
+    else:
+        if len(data) < 84:
+            raise LoadError("short header")
+        n = int.from_bytes(data[80:84], "little")
+        if len(data) < 84 + 50 * n:
+            raise LoadError("short file")
+        rec = np.frombuffer(data, dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("a", "<u2")]),
+                            count=n, offset=84)
+        tris = rec["v"].astype(np.float32)
     flat = tris.reshape(-1, 3)
     m = _mesh(flat[:, 0], flat[:, 1], flat[:, 2], None, np.tile(np.array([255, 255, 0], np.uint8), (tris.shape[0], 1)))
     m["bbox_max"] = np.max(tris.reshape(-1, 3), axis=0).astype(np.float32) if tris.size else \
