@@ -85,6 +85,9 @@ void sloth_viewport_transform(uint16_t width, uint16_t height, float extent, flo
  * Context::blank(image=false) (src/context.rs:22-34): 0x0 viewport, identity
  * utransform. */
 sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream);
+/* Destroys the context.  Batches made on it lose their device memory; they and the
+ * context's meshes stay valid handles only for sloth_batch_destroy / sloth_mesh_destroy
+ * (a mesh also keeps drawing on other contexts of its device). */
 void sloth_ctx_destroy(sloth_ctx *ctx);
 
 /* Text of the last error on this context ("" when none). */

@@ -75,6 +75,8 @@ struct sloth_batch {
 // Shared with sloth_api.cu.
 extern "C++" {
 sloth_status sloth_ctx_fail(sloth_ctx *ctx, sloth_status st, const char *msg);
+void sloth_ctx_register_batch(sloth_ctx *ctx, sloth_batch *b);
+void sloth_ctx_unregister_batch(sloth_ctx *ctx, sloth_batch *b);
 int sloth_ctx_device(const sloth_ctx *ctx);
 cudaStream_t sloth_ctx_stream(const sloth_ctx *ctx);
 int sloth_ctx_depth_cull(const sloth_ctx *ctx);
@@ -423,6 +425,27 @@ sloth_status diff_prepare(sloth_batch *b, const float *vertex_rgb, const float *
 
 }  // namespace
 
+// Release a batch's device and pinned memory and cut it from its context (its context is
+// being destroyed, or the batch is).  The handle stays valid for sloth_batch_destroy.
+void sloth_batch_detach(sloth_batch *b)
+{
+    if (!b->ctx) return;
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->stream);
+    free_layout(b);
+    bfree(b->diff_blk);
+    bfree(b->vis);
+    flush_release(b->flush);
+    if (b->h_mats) cudaFreeHost(b->h_mats);
+    if (b->h_total) cudaFreeHost(b->h_total);
+    if (b->h_overflow) cudaFreeHost(b->h_overflow);
+    b->h_mats = nullptr;
+    b->h_total = b->h_overflow = nullptr;
+    b->ctx = nullptr;
+    b->stream = nullptr;
+    b->rendered = false;
+}
+
 extern "C" {
 
 sloth_status sloth_batch_create(sloth_ctx *ctx, const sloth_frame_desc *frames, uint32_t nframes,
@@ -460,9 +483,11 @@ sloth_status sloth_batch_create(sloth_ctx *ctx, const sloth_frame_desc *frames, 
     if (cudaMallocHost(&b->h_mats, (ndraws ? ndraws : 1) * sizeof(Mat4)) != cudaSuccess ||
         cudaMallocHost(&b->h_total, 4) != cudaSuccess || cudaMallocHost(&b->h_overflow, 4) != cudaSuccess ||
         prepare_batch_kernels() != cudaSuccess) {
-        sloth_batch_destroy(b);
+        sloth_batch_detach(b);
+        delete b;
         return sloth_ctx_fail(ctx, SLOTH_ERR_OUT_OF_MEMORY, "batch host buffers");
     }
+    sloth_ctx_register_batch(ctx, b);
     set_mats(b);
     const sloth_status st = build(b, 0);
     if (st != SLOTH_OK) {
@@ -476,21 +501,16 @@ sloth_status sloth_batch_create(sloth_ctx *ctx, const sloth_frame_desc *frames, 
 void sloth_batch_destroy(sloth_batch *b)
 {
     if (!b) return;
-    cudaSetDevice(b->device);
-    cudaStreamSynchronize(b->stream);
-    free_layout(b);
-    bfree(b->diff_blk);
-    bfree(b->vis);
-    flush_release(b->flush);
-    if (b->h_mats) cudaFreeHost(b->h_mats);
-    if (b->h_total) cudaFreeHost(b->h_total);
-    if (b->h_overflow) cudaFreeHost(b->h_overflow);
+    if (b->ctx) {
+        sloth_ctx_unregister_batch(b->ctx, b);
+        sloth_batch_detach(b);
+    }
     delete b;
 }
 
 sloth_status sloth_batch_set_transforms(sloth_batch *b, const float *transforms)
 {
-    if (!b || !transforms) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx || !transforms) return SLOTH_ERR_INVALID_ARGUMENT;
     BCU(b, cudaSetDevice(b->device));
     BCU(b, cudaStreamSynchronize(b->stream));   // the previous render has read the matrices
     memcpy(b->transforms.data(), transforms, b->transforms.size() * sizeof(float));
@@ -500,7 +520,7 @@ sloth_status sloth_batch_set_transforms(sloth_batch *b, const float *transforms)
 
 sloth_status sloth_batch_render(sloth_batch *b)
 {
-    if (!b) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx) return SLOTH_ERR_INVALID_ARGUMENT;
     BCU(b, cudaSetDevice(b->device));
     b->vis_valid = false;
     if (!b->rendered || !b->bb.entries) return render_planned(b);
@@ -517,7 +537,7 @@ sloth_status sloth_batch_render(sloth_batch *b)
 
 sloth_status sloth_batch_read(sloth_batch *b, uint32_t frame, uint32_t *cells, float *z, int32_t *winner)
 {
-    if (!b || frame >= b->frames.size()) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx || frame >= b->frames.size()) return SLOTH_ERR_INVALID_ARGUMENT;
     if (!b->rendered) return sloth_ctx_fail(b->ctx, SLOTH_ERR_INVALID_ARGUMENT, "render the batch first");
     BCU(b, cudaSetDevice(b->device));
     sloth_status st = settle(b);
@@ -536,7 +556,7 @@ sloth_status sloth_batch_read(sloth_batch *b, uint32_t frame, uint32_t *cells, f
 sloth_status sloth_batch_flush(sloth_batch *b, uint32_t frame, int format, char *out, uint64_t capacity,
                                uint64_t *bytes)
 {
-    if (!b || frame >= b->frames.size() || !bytes) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx || frame >= b->frames.size() || !bytes) return SLOTH_ERR_INVALID_ARGUMENT;
     if (format < SLOTH_FLUSH_PLAIN || format > SLOTH_FLUSH_HTML)
         return sloth_ctx_fail(b->ctx, SLOTH_ERR_INVALID_ARGUMENT, "unknown flush format");
     if (!b->rendered) return sloth_ctx_fail(b->ctx, SLOTH_ERR_INVALID_ARGUMENT, "render the batch first");
@@ -555,7 +575,7 @@ sloth_status sloth_batch_flush(sloth_batch *b, uint32_t frame, int format, char 
 
 sloth_status sloth_batch_frame_buffers(sloth_batch *b, uint32_t frame, const uint32_t **cells, const float **z)
 {
-    if (!b || frame >= b->frames.size()) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx || frame >= b->frames.size()) return SLOTH_ERR_INVALID_ARGUMENT;
     if (cells) *cells = b->cells + b->cell_off[frame];
     if (z) *z = b->z + b->z_off[frame];
     return SLOTH_OK;
@@ -563,7 +583,7 @@ sloth_status sloth_batch_frame_buffers(sloth_batch *b, uint32_t frame, const uin
 
 sloth_status sloth_batch_fragments(sloth_batch *b, uint64_t *fragments)
 {
-    if (!b || !fragments) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx || !fragments) return SLOTH_ERR_INVALID_ARGUMENT;
     BCU(b, cudaSetDevice(b->device));
     sloth_status st = settle(b);
     if (st != SLOTH_OK) return st;
@@ -575,7 +595,7 @@ sloth_status sloth_batch_fragments(sloth_batch *b, uint64_t *fragments)
 
 sloth_status sloth_batch_set_tile_shape(sloth_batch *b, int shape)
 {
-    if (!b || shape < 0 || shape >= kNumTileShapes) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx || shape < 0 || shape >= kNumTileShapes) return SLOTH_ERR_INVALID_ARGUMENT;
     BCU(b, cudaSetDevice(b->device));
     BCU(b, cudaStreamSynchronize(b->stream));
     return shape == b->shape ? SLOTH_OK : build(b, shape);
@@ -583,7 +603,7 @@ sloth_status sloth_batch_set_tile_shape(sloth_batch *b, int shape)
 
 sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, float *best_ms)
 {
-    if (!b) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx) return SLOTH_ERR_INVALID_ARGUMENT;
     if (reps < 1) reps = 3;
     BCU(b, cudaSetDevice(b->device));
     cudaEvent_t e0, e1;
@@ -626,7 +646,7 @@ sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, flo
 
 sloth_status sloth_batch_depth_cells(sloth_batch *b, uint32_t frame, uint64_t *first, uint64_t *count)
 {
-    if (!b || frame >= b->frames.size()) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx || frame >= b->frames.size()) return SLOTH_ERR_INVALID_ARGUMENT;
     if (first) *first = b->z_off[frame];
     if (count) *count = b->z_off[frame + 1] - b->z_off[frame];
     return SLOTH_OK;
@@ -635,7 +655,7 @@ sloth_status sloth_batch_depth_cells(sloth_batch *b, uint32_t frame, uint64_t *f
 sloth_status sloth_batch_shade(sloth_batch *b, const float *vertex_rgb, const float *light, float *rgb,
                                int store_visibility)
 {
-    if (!b || !rgb) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx || !rgb) return SLOTH_ERR_INVALID_ARGUMENT;
     sloth_status st = diff_prepare(b, vertex_rgb, light);
     if (st != SLOTH_OK) return st;
     if (store_visibility && !b->vis) BCU(b, balloc(&b->vis, b->total_z));
@@ -649,7 +669,7 @@ sloth_status sloth_batch_shade_backward(sloth_batch *b, const float *vertex_rgb,
                                         const float *grad_rgb, float *grad_pos, float *grad_vertex_rgb,
                                         float *grad_light)
 {
-    if (!b || !grad_rgb) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (!b || !b->ctx || !grad_rgb) return SLOTH_ERR_INVALID_ARGUMENT;
     sloth_status st = diff_prepare(b, vertex_rgb, light);
     if (st != SLOTH_OK) return st;
     BCU(b, launch_batch_shade_backward(dev_view(b), b->diff_blk, b->ndiff_blk, vertex_rgb, light, grad_rgb,

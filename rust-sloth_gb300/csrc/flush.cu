@@ -35,7 +35,7 @@ __device__ __forceinline__ uint32_t cell_bytes(uint32_t cell, int format)
 {
     if (format == kFlushPlain) return 1;
     const uint32_t d = ndigits((cell >> 8) & 255u) + ndigits((cell >> 16) & 255u) + ndigits(cell >> 24);
-    return format == kFlushAnsi ? 31u + d : 28u + d;
+    return format == kFlushAnsi ? 31u + d : 29u + d;
 }
 
 __device__ __forceinline__ uint32_t put_str(char *o, const char *s)

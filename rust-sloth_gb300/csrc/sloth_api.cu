@@ -9,6 +9,7 @@
 // Host float math below must be compiled with -ffp-contract=off (see build.py).
 #include "sloth_gpu.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -35,6 +36,9 @@ struct KernelClock {
 };
 
 }  // namespace
+
+// batch_api.cu: frees a batch's device memory and cuts it from its context.
+void sloth_batch_detach(sloth_batch *b);
 
 struct sloth_mesh {
     sloth_ctx *ctx = nullptr;
@@ -80,6 +84,10 @@ struct sloth_ctx {
     uint64_t launches = 0;
 
     FlushScratch flush;
+
+    // handles made on this context: released or detached when it is destroyed
+    std::vector<sloth_mesh *> meshes;
+    std::vector<sloth_batch *> batches;
 };
 
 // ---------------------------------------------------------------------------------------
@@ -245,6 +253,12 @@ static sloth_status resolve_pending(sloth_ctx *ctx)
 // accessors for the batch API (batch_api.cu)
 // ---------------------------------------------------------------------------------------
 sloth_status sloth_ctx_fail(sloth_ctx *ctx, sloth_status st, const char *msg) { return fail(ctx, st, "%s", msg); }
+void sloth_ctx_register_batch(sloth_ctx *ctx, sloth_batch *b) { ctx->batches.push_back(b); }
+void sloth_ctx_unregister_batch(sloth_ctx *ctx, sloth_batch *b)
+{
+    auto &v = ctx->batches;
+    v.erase(std::remove(v.begin(), v.end(), b), v.end());
+}
 int sloth_ctx_device(const sloth_ctx *ctx) { return ctx->device; }
 cudaStream_t sloth_ctx_stream(const sloth_ctx *ctx) { return ctx->stream; }
 int sloth_ctx_depth_cull(const sloth_ctx *ctx) { return ctx->depth_cull; }
@@ -374,6 +388,10 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    // batches lose their device memory and meshes their context; destroying either
+    // afterwards only frees what is left
+    for (sloth_batch *b : ctx->batches) sloth_batch_detach(b);
+    for (sloth_mesh *m : ctx->meshes) m->ctx = nullptr;
     for (auto &kv : ctx->clocks)
         for (auto &ev : kv.second.pending) {
             cudaEventDestroy(ev.a);
@@ -599,6 +617,7 @@ sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, c
             }
         memcpy(m->bbox_max, b, sizeof b);
     }
+    ctx->meshes.push_back(m);
     *out = m;
     return SLOTH_OK;
 }
@@ -606,6 +625,10 @@ sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, c
 void sloth_mesh_destroy(sloth_mesh *m)
 {
     if (!m) return;
+    if (m->ctx) {
+        auto &v = m->ctx->meshes;
+        v.erase(std::remove(v.begin(), v.end(), m), v.end());
+    }
     cudaSetDevice(m->device);
     dfree(m->x);
     dfree(m->y);

@@ -149,3 +149,28 @@ def test_batch_dense_frames_split_tiles(ctx):
     b.render()
     check_frames(b, meshes, frames, "graph")
     b.close()
+
+
+def test_context_destroyed_before_its_batch_and_mesh():
+    """Destroying a context detaches its batches and meshes: later calls on the batch
+    fail cleanly and destroying the handles is safe (the meshes' buffers stay usable)."""
+    c = S.Context(0)
+    m = W.soup(300, seed=51)
+    dm = dev_mesh(c, m)
+    U = O.viewport_transform(40, 20, O.scene_extent([m["bbox_max"]]))
+    b = S.Batch(c, [{"w": 40, "h": 20, "image": True, "U": U, "draws": [(dm, O.euler_rotation(0.0, 3.1, 0.0))]}])
+    b.render()
+    c2 = S.Context(0)
+    c.close()
+    with pytest.raises(S.SlothError):
+        b.render()
+    # the mesh still draws on another context of the same device
+    c2.set_viewport(40, 20, True)
+    c2.set_utransform(U)
+    c2.clear()
+    c2.draw_mesh(dm, O.euler_rotation(0.0, 3.1, 0.0))
+    ref = oracle_render([m], O.euler_rotation(0.0, 3.1, 0.0), 40, 20, True, U=U)
+    assert np.array_equal(c2.read()[0], ref.cells)
+    b.close()
+    dm.close()
+    c2.close()
