@@ -225,6 +225,9 @@ def run_gpu(args):
     # which events recorded on stream 0 do not bracket.
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
+    if args.only_batched:
+        print(json.dumps({"batched": run_config3(torch, stream, local, args)}), flush=True)
+        return 0
     if args.only_diff:
         print(json.dumps({"differentiable": run_config4(torch, stream, local, args),
                           "inverse_rendering": run_config5(torch, stream, local, args)}), flush=True)
@@ -413,7 +416,11 @@ def run_config3(torch, stream, device, args):
     frames = [{"w": w, "h": h, "image": im, "U": U, "draws": [(dev[mi], R)]} for mi, w, h, im, U, R in specs]
     batch = S.Batch(ctx, frames)
     batch.render()
-    shape, _ = batch.autotune(reps=2)
+    if args.batched_shape >= 0:
+        shape = args.batched_shape
+        batch.set_tile_shape(shape)
+    else:
+        shape, _ = batch.autotune(reps=2)
     batch.render()
     torch.cuda.synchronize()
     steps = max(3, args.batched_steps)
@@ -672,6 +679,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched config-3 leg")
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable legs (configs 4 and 5)")
+    ap.add_argument("--only-batched", action="store_true", help="run only the batched config-3 leg")
+    ap.add_argument("--batched-shape", type=int, default=-1,
+                    help="tile shape of the config-3 batch (default: autotuned)")
     ap.add_argument("--only-diff", action="store_true", help="run only the differentiable legs (configs 4 and 5)")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     args = ap.parse_args()
