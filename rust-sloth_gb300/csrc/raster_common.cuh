@@ -9,12 +9,14 @@
 // depth write.  Keys of earlier draws since the clear are merged in first.
 //
 // Depth culling (on by default): entries carry a proven lower bound of every depth their
-// triangle can produce in this tile (bounds.cuh).  The CTA sorts its entries on that
-// bound (front to back) and keeps an upper bound of the farthest key depth among the
-// tile's writable cells.  An entry whose bound is strictly above it cannot win any cell,
-// and neither can the entries sorted after it, so the warps stop there.  Only skipped
-// work changes: the buffers are the same bit for bit; the fragment counter then counts
-// only the fragments of the triangles that were rasterized.
+// triangle can produce in this tile (bounds.cuh).  The CTA orders its entries front to
+// back by a counting sort into depth buckets (one pass of shared atomics, not a sorting
+// network) and keeps an upper bound of the farthest key depth among the tile's writable
+// cells.  An entry whose bound is strictly above it cannot win any cell; when the
+// smallest bound of the bucket a window of entries starts in is above it, neither can
+// any entry left, so the warps stop there.  Only skipped work changes: the buffers are
+// the same bit for bit; the fragment counter then counts only the fragments of the
+// triangles that were rasterized.
 #pragma once
 
 #include "sloth_internal.cuh"
@@ -22,14 +24,20 @@
 
 namespace sloth {
 
-constexpr int kSortCap = 2048;   // entries sorted per pass (16 KB of shared memory)
+constexpr int kSortCap = 2048;   // entries ordered per pass (16 KB of shared memory)
+constexpr int kDepthBuckets = 256;   // depth buckets of the counting sort (= kRasterThreads)
 constexpr int kRasterThreads = 256;
+static_assert(kDepthBuckets == kRasterThreads, "one bucket per thread in the scan");
 constexpr int kRasterMinBlocks = 5;   // resident CTAs per SM the register budget allows
 
 template <int TW, int TH>
 struct TileSmem {
     unsigned long long keys[TH * TW];
     unsigned long long ent[kSortCap];
+    uint32_t bcount[kDepthBuckets];     // entries per depth bucket, then the scatter cursors
+    uint32_t bstart[kDepthBuckets + 1]; // first entry of each bucket (exclusive scan)
+    uint32_t bmin[kDepthBuckets];       // smallest depth bound in each bucket
+    uint32_t zlo_min, zlo_max;
     uint32_t next, zmax_u, zmax_w;
     uint32_t frags[kRasterThreads / 32];
 };
@@ -182,39 +190,101 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
     const int wid = threadIdx.x >> 5;
     for (uint32_t base = 0; base < cnt; base += kSortCap) {
         const uint32_t n = min(cnt - base, (uint32_t)kSortCap);
-        uint32_t np2 = 2;
-        while (np2 < n) np2 <<= 1;
-        for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) S.ent[i] = i < n ? entries[base + i] : ~0ull;
+        if (!depth_cull) {
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) S.ent[i] = entries[base + i];
+        } else {
+            // Counting sort into kDepthBuckets buckets of the entries' depth bounds (front
+            // to back): a bucket function monotone in the bound, so that bucket b's
+            // smallest bound (bmin) grows with b; the order inside a bucket is free.
+            if (threadIdx.x == 0) {
+                S.zlo_min = 0xffffffffu;
+                S.zlo_max = 0u;
+            }
+            S.bcount[threadIdx.x] = 0u;
+            S.bmin[threadIdx.x] = 0xffffffffu;
+            block_sync();
+            // range of the finite bounds (-inf bounds, of triangles without a usable
+            // bound, go to bucket 0)
+            uint32_t lmin = 0xffffffffu, lmax = 0u;
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                const uint32_t z = (uint32_t)(entries[base + i] >> 32);
+                if (isfinite(float_of_ordered(z))) {
+                    lmin = min(lmin, z);
+                    lmax = max(lmax, z);
+                }
+            }
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) {
+                lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, d));
+                lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, d));
+            }
+            if (lane == 0) {
+                atomicMin(&S.zlo_min, lmin);
+                atomicMax(&S.zlo_max, lmax);
+            }
+            block_sync();
+            // buckets linear in depth over [fmin, fmax]: monotone in the bound
+            const bool any = S.zlo_min <= S.zlo_max;
+            const float fmin = any ? float_of_ordered(S.zlo_min) : 0.0f;
+            const float fspan = any ? float_of_ordered(S.zlo_max) - fmin : 0.0f;
+            const float scale = fspan > 0.0f ? (float)kDepthBuckets / fspan : 0.0f;
+            auto bucket = [&](uint32_t z) {
+                const float f = float_of_ordered(z);
+                if (!(f > fmin)) return 0u;
+                const float q = (f - fmin) * scale;
+                return q < (float)(kDepthBuckets - 1) ? (uint32_t)q : (uint32_t)kDepthBuckets - 1;
+            };
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                const uint32_t z = (uint32_t)(entries[base + i] >> 32);
+                const uint32_t b = bucket(z);
+                atomicAdd(&S.bcount[b], 1u);
+                atomicMin(&S.bmin[b], z);
+            }
+            block_sync();
+            {
+                // exclusive scan of the 256 counts, one per thread
+                __shared__ uint32_t ws[kRasterThreads / 32];
+                const uint32_t v = S.bcount[threadIdx.x];
+                uint32_t x = v;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t o = __shfl_up_sync(0xffffffffu, x, d);
+                    if (lane >= d) x += o;
+                }
+                if (lane == 31) ws[wid] = x;
+                block_sync();
+                uint32_t pre = x - v;
+                for (int w = 0; w < wid; ++w) pre += ws[w];
+                S.bstart[threadIdx.x] = pre;
+                S.bcount[threadIdx.x] = pre;   // scatter cursor
+                if (threadIdx.x == 0) S.bstart[kDepthBuckets] = n;
+            }
+            block_sync();
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                const unsigned long long e = entries[base + i];
+                S.ent[atomicAdd(&S.bcount[bucket((uint32_t)(e >> 32))], 1u)] = e;
+            }
+        }
         if (threadIdx.x == 0) S.next = 0;
         block_sync();
-        if (depth_cull) {
-            // bitonic sort, ascending: front-to-back depth bounds
-            for (uint32_t k = 2; k <= np2; k <<= 1)
-                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                    for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x) {
-                        const uint32_t ixj = i ^ j;
-                        if (ixj > i) {
-                            const unsigned long long a = S.ent[i], b = S.ent[ixj];
-                            if ((a > b) == ((i & k) == 0)) {
-                                S.ent[i] = b;
-                                S.ent[ixj] = a;
-                            }
-                        }
-                    }
-                    block_sync();
-                }
-        }
         // Windows of kRasterThreads sorted entries; lane i of warp w takes entry w + 8i, so
         // that the warps move through the sorted order together.  Each lane loads its own
         // record; a small triangle is walked by its lane, a larger one by the whole warp
         // (in the warp's sorted order, each checked against the depth bound right before
         // it).
-        bool stop = false;        // warp-uniform: the rest of this warp's entries are hidden
+        uint32_t wb = 0;          // warp-uniform: the bucket of the current window's first entry
         // warp-uniform count of warp walks since the warp's last refresh of the bound: one
         // refresh per 16 walks of a warp (about one per 16 entries of the CTA, as the
         // warps take turns), warp w's first after 2 + 2w walks
         uint32_t since = 14u - 2u * (uint32_t)wid;
-        for (uint32_t w0 = 0; w0 < n && !stop; w0 += kRasterThreads) {
+        for (uint32_t w0 = 0; w0 < n; w0 += kRasterThreads) {
+            if (depth_cull) {
+                // every entry from here on lies in bucket wb or later: when that bucket's
+                // smallest bound is behind every writable cell, so is everything left
+                while (S.bstart[wb + 1] <= w0) ++wb;
+                const uint32_t zu = *(volatile uint32_t *)&S.zmax_u, zw = *(volatile uint32_t *)&S.zmax_w;
+                if (S.bmin[wb] > max(zu, zw)) break;
+            }
             const uint32_t e = w0 + wid + (kRasterThreads / 32) * lane;
             const unsigned long long ent = e < n ? S.ent[e] : ~0ull;
             bool live = e < n;
@@ -255,20 +325,12 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                     ++since;
                     // lane 0 decides for the warp (the bounds may move between reads)
                     const unsigned long long es = __shfl_sync(0xffffffffu, ent, src);
-                    uint32_t verdict = 0;
+                    uint32_t hidden = 0;
                     if (lane == 0) {
-                        const uint32_t zlo = (uint32_t)(es >> 32);
                         const uint32_t zu = *(volatile uint32_t *)&S.zmax_u, zw = *(volatile uint32_t *)&S.zmax_w;
-                        const uint32_t lim = ((uint32_t)es & 0x80000000u) ? max(zu, zw) : zu;
-                        verdict = zlo > max(zu, zw) ? 2u : (zlo > lim ? 1u : 0u);
+                        hidden = (uint32_t)(es >> 32) > (((uint32_t)es & 0x80000000u) ? max(zu, zw) : zu);
                     }
-                    verdict = __shfl_sync(0xffffffffu, verdict, 0);
-                    if (verdict == 2u) {
-                        // sorted: every later entry of this warp is behind every writable cell
-                        stop = true;
-                        break;
-                    }
-                    if (verdict == 1u) continue;
+                    if (__shfl_sync(0xffffffffu, hidden, 0)) continue;
                 }
                 const uint32_t gt = __shfl_sync(0xffffffffu, gtri, src);
                 const TriRecord r = load_record(fb.records, gt);

@@ -112,6 +112,11 @@ __device__ __forceinline__ uint32_t ordered_z(float z)
     if (b == 0x80000000u) b = 0u;                     // -0 -> +0
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
+// The float of an ordered depth (ordered_z's inverse, -0 read as +0).
+__device__ __forceinline__ float float_of_ordered(uint32_t o)
+{
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
 __device__ __forceinline__ uint64_t make_key(float z, uint32_t tri, uint32_t not_wrapped)
 {
     return ((uint64_t)ordered_z(z) << 32) | (uint64_t)((tri << 1) | not_wrapped);
