@@ -12,7 +12,9 @@ A step = one frame: clear + draw_mesh + resolve of the depth/frame buffers.
           library's stream, L2 flushed (512 MiB write) before every timed step.
   e2e   : frames/s through the public C ABI with host buffers: every step uploads the
           mesh from pinned host memory (sloth_mesh_update), draws, and reads the frame and
-          depth buffers back to pinned host memory (sloth_ctx_read).
+          depth buffers back to pinned host memory.  Two contexts take the frames in turn
+          (sloth_ctx_read_async), so a frame's read-back overlaps the next frame's upload
+          and draw; `serial_value` is the same with one context and a blocking read.
 `--impl reference` times the reference algorithm (the CPU oracle restating
 src/rasterizer.rs, banded over all host threads) on a bounded sample of the same frame.
 One JSON line on stdout (rank 0).
@@ -298,33 +300,70 @@ def run_gpu(args):
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     hx, hy, hz, hrgb = pin(m["x"]), pin(m["y"]), pin(m["z"]), pin(m["rgb"].reshape(-1))
     nf, nz = ctx.sizes()
-    hcells = torch.empty(nf, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
-    hzbuf = torch.empty(nz, dtype=torch.float32).pin_memory().numpy()
     h2d = hx.nbytes + hy.nbytes + hz.nbytes + hrgb.nbytes
-    d2h = hcells.nbytes + hzbuf.nbytes
+    d2h = nf * 4 + nz * 4
 
-    def e2e_step():
-        dm.update(hx, hy, hz, hrgb)
-        ctx.clear()
-        ctx.draw_mesh(dm, R)
-        ctx.read_into(hcells, hzbuf)
+    def host_out():
+        return (torch.empty(nf, dtype=torch.int32).pin_memory().numpy().view(np.uint32),
+                torch.empty(nz, dtype=torch.float32).pin_memory().numpy())
 
     e2e = None
     if not args.no_e2e:
+        # serial: upload, draw, read back, one frame at a time on one context
+        hc, hzb = host_out()
+
+        def serial_step():
+            dm.update(hx, hy, hz, hrgb)
+            ctx.clear()
+            ctx.draw_mesh(dm, R)
+            ctx.read_into(hc, hzb)
+
         for _ in range(max(1, args.warmup)):
-            e2e_step()
+            serial_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            serial_step()
+        serial_s = time.perf_counter() - t0
+        # pipelined: two contexts in turn, each with its own mesh buffers and host outputs;
+        # a frame's read-back overlaps the next frame's upload and draw
+        ctx2 = S.Context(local)
+        ctx2.set_viewport(W_PX, H_PX, True)
+        dm2 = S.Mesh(ctx2, m["x"], m["y"], m["z"], m["rgb"])
+        ctx2.update([dm2])
+        ctx2.set_depth_cull(not args.no_depth_cull)
+        lanes = [(ctx, dm, *host_out()), (ctx2, dm2, *host_out())]
+
+        def pipelined_step(i):
+            c, mm, oc, oz = lanes[i & 1]
+            c.synchronize()            # this context's previous frame (and its read-back) is done
+            mm.update(hx, hy, hz, hrgb)
+            c.clear()
+            c.draw_mesh(mm, R)
+            c.read_into_async(oc, oz)
+
+        for i in range(max(2, args.warmup)):
+            pipelined_step(i)
+        ctx.synchronize()
+        ctx2.synchronize()
         if ws > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
+        for i in range(args.steps):
+            pipelined_step(i)
+        ctx.synchronize()
+        ctx2.synchronize()
         e2e_s = time.perf_counter() - t0
+        # the pipelined frames equal the serial ones
+        assert np.array_equal(lanes[0][2], hc) and np.array_equal(lanes[1][2], hc)
         if ws > 1:
-            t = torch.tensor([e2e_s], device=dev)
+            t = torch.tensor([e2e_s, serial_s], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t.item())
+            e2e_s, serial_s = float(t[0].item()), float(t[1].item())
         e2e = {"value": ws * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h}
+               "d2h_bytes_per_step": d2h,
+               "pipeline": "two contexts in turn: a frame's read-back overlaps the next frame's upload and draw",
+               "serial_value": ws * args.steps / serial_s}
+        ctx2.close()
 
     if rank != 0:
         if ws > 1:

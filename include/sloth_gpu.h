@@ -119,6 +119,14 @@ sloth_status sloth_ctx_sizes(const sloth_ctx *ctx, uint64_t *frame_cells, uint64
  * Blocks until the copies complete. */
 sloth_status sloth_ctx_read(sloth_ctx *ctx, uint32_t *cells, float *z, int32_t *winner);
 
+/* sloth_ctx_read without waiting: the copies are queued on the context's stream (host
+ * buffers should be page-locked) and complete by the next sloth_ctx_synchronize.  With
+ * two contexts used in turn, one frame's read-back overlaps the next frame's upload and
+ * draw.  Not in the reference, whose Context is synchronous. */
+sloth_status sloth_ctx_read_async(sloth_ctx *ctx, uint32_t *cells, float *z, int32_t *winner);
+/* Wait for everything queued on the context's stream. */
+sloth_status sloth_ctx_synchronize(sloth_ctx *ctx);
+
 /* Device pointers of the resolved buffers (valid until the next clear/resize/destroy),
  * for consumers that stay on the GPU.  Resolves pending draws first (asynchronously). */
 sloth_status sloth_ctx_device_buffers(sloth_ctx *ctx, const uint32_t **cells, const float **z);

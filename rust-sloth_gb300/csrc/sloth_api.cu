@@ -535,6 +535,32 @@ sloth_status sloth_ctx_flush_device(sloth_ctx *ctx, int format, const char **dev
     return SLOTH_OK;
 }
 
+sloth_status sloth_ctx_read_async(sloth_ctx *ctx, uint32_t *cells, float *z, int32_t *winner)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    CU(ctx, cudaSetDevice(ctx->device));
+    sloth_status st = resolve_pending(ctx);
+    if (st != SLOTH_OK) return st;
+    const size_t nz = (size_t)ctx->g.w * ctx->g.h;
+    const size_t ncells = ctx->g.image ? nz + ctx->g.h : nz;
+    if (cells)
+        CU(ctx, cudaMemcpyAsync(cells, ctx->fb.cells_out, ncells * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+    if (z) CU(ctx, cudaMemcpyAsync(z, ctx->fb.z_out, nz * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    if (winner)
+        CU(ctx, cudaMemcpyAsync(winner, ctx->fb.winner_out, nz * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+    return SLOTH_OK;
+}
+
+sloth_status sloth_ctx_synchronize(sloth_ctx *ctx)
+{
+    if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    CU(ctx, cudaSetDevice(ctx->device));
+    CU(ctx, cudaStreamSynchronize(ctx->stream));
+    return SLOTH_OK;
+}
+
 sloth_status sloth_ctx_device_buffers(sloth_ctx *ctx, const uint32_t **cells, const float **z)
 {
     if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;

@@ -72,6 +72,8 @@ SIGNATURES = {
     "sloth_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "sloth_batch_depth_cells": (C.c_int, [_vp, C.c_uint32, _u64p, _u64p]),
     "sloth_ctx_flush": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_uint64, _u64p]),
+    "sloth_ctx_read_async": (C.c_int, [_vp, _u32p, _f32p, _i32p]),
+    "sloth_ctx_synchronize": (C.c_int, [_vp]),
     "sloth_ctx_flush_device": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_void_p), _u64p]),
     "sloth_batch_flush": (C.c_int, [_vp, C.c_uint32, C.c_int, C.c_char_p, C.c_uint64, _u64p]),
     "sloth_batch_shade": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int]),
@@ -224,6 +226,14 @@ class Context:
 
     def read_into(self, cells: np.ndarray | None, z: np.ndarray | None):
         self._check(self.lib.sloth_ctx_read(self.h, _ptr(cells, C.c_uint32), _ptr(z, C.c_float), None))
+
+    def read_into_async(self, cells: np.ndarray | None, z: np.ndarray | None):
+        """Queue the copies (complete at the next synchronize); keep the arrays alive."""
+        self._pending = (cells, z)
+        self._check(self.lib.sloth_ctx_read_async(self.h, _ptr(cells, C.c_uint32), _ptr(z, C.c_float), None))
+
+    def synchronize(self):
+        self._check(self.lib.sloth_ctx_synchronize(self.h))
 
     def device_buffers(self):
         c, z = C.c_void_p(), C.c_void_p()
