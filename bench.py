@@ -56,6 +56,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(values, device, ws: int):
+    """Element-wise maximum of per-rank timings (replicas: the slowest rank sets the job's
+    time); no-op on one rank.  `device`: cuda for NCCL, cpu for gloo."""
+    if ws <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def whole_job_rate(units_per_rank: int, ws: int, seconds: float) -> float:
+    """Weak scaling over replicas: every rank processes `units_per_rank` units; the job's
+    rate is all ranks' units over the slowest rank's time."""
+    return ws * units_per_rank / seconds
+
+
 WORKLOADS = {
     # name: (description, width, height, small triangles, large triangles)
     "config2": (WORKLOAD, 3840, 2160, 1_000_000, 2_000),
@@ -288,13 +306,9 @@ def run_gpu(args):
         if n:
             kernels[name] = {"ms_per_launch": t / n, "launches": n}
     ctx.set_timing(False)
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks([ms], dev, ws)[0]
     ms_per_step = ms / args.steps
-    fps_per_gpu = 1000.0 / ms_per_step
-    value = fps_per_gpu * ws
+    value = whole_job_rate(args.steps, ws, ms / 1000.0)
 
     # ---- end to end through the C ABI with host buffers
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -355,14 +369,11 @@ def run_gpu(args):
         e2e_s = time.perf_counter() - t0
         # the pipelined frames equal the serial ones
         assert np.array_equal(lanes[0][2], hc) and np.array_equal(lanes[1][2], hc)
-        if ws > 1:
-            t = torch.tensor([e2e_s, serial_s], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s, serial_s = float(t[0].item()), float(t[1].item())
-        e2e = {"value": ws * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+        e2e_s, serial_s = max_over_ranks([e2e_s, serial_s], dev, ws)
+        e2e = {"value": whole_job_rate(args.steps, ws, e2e_s), "unit": "frames/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h,
                "pipeline": "two contexts in turn: a frame's read-back overlaps the next frame's upload and draw",
-               "serial_value": ws * args.steps / serial_s}
+               "serial_value": whole_job_rate(args.steps, ws, serial_s)}
         ctx2.close()
 
     if rank != 0:
