@@ -37,7 +37,8 @@ typedef enum sloth_status {
     SLOTH_ERR_OUT_OF_MEMORY = 2,
     SLOTH_ERR_CUDA = 3,
     SLOTH_ERR_LIMIT = 4,          /* a size beyond a documented limit */
-    SLOTH_ERR_DEVICE_FAULT = 5    /* a kernel reported an internal error flag */
+    SLOTH_ERR_DEVICE_FAULT = 5    /* a kernel gave up waiting for one of its copies (reported
+                                     by the next synchronising call; the frame is invalid) */
 } sloth_status;
 
 typedef struct sloth_ctx sloth_ctx;

@@ -57,6 +57,8 @@ struct sloth_batch {
     uint32_t *overflow = nullptr;
     uint32_t *h_total = nullptr;              // pinned
     uint32_t *h_overflow = nullptr;           // pinned
+    uint32_t *error = nullptr;                // device error word of the raster (sticky)
+    uint32_t *h_error = nullptr;              // pinned
     int2 *blk[4] = {nullptr, nullptr, nullptr, nullptr};   // vertex, triangle, newline, resolve
     uint32_t nblk[4] = {0, 0, 0, 0};
 
@@ -271,6 +273,7 @@ sloth_status build(sloth_batch *b, int shape)
         bf.fb.cells_out = b->cells + b->cell_off[f];
         bf.fb.winner_out = b->winner + b->z_off[f];
         bf.fb.fragments = b->fragments;
+        bf.fb.error = b->error;
         bf.fb.gen = 1;
     }
     BCU(b, balloc(&b->d_frames, nf));
@@ -389,7 +392,10 @@ sloth_status capture(sloth_batch *b)
 sloth_status settle(sloth_batch *b)
 {
     BCU(b, cudaMemcpyAsync(b->h_overflow, b->overflow, 4, cudaMemcpyDeviceToHost, b->stream));
+    BCU(b, cudaMemcpyAsync(b->h_error, b->error, 4, cudaMemcpyDeviceToHost, b->stream));
     BCU(b, cudaStreamSynchronize(b->stream));
+    if (*b->h_error)
+        return sloth_ctx_fail(b->ctx, SLOTH_ERR_DEVICE_FAULT, "a raster block gave up waiting for its tile copy");
     if (*b->h_overflow) {
         sloth_status st = render_planned(b);
         if (st != SLOTH_OK) return st;
@@ -439,8 +445,10 @@ void sloth_batch_detach(sloth_batch *b)
     if (b->h_mats) cudaFreeHost(b->h_mats);
     if (b->h_total) cudaFreeHost(b->h_total);
     if (b->h_overflow) cudaFreeHost(b->h_overflow);
+    if (b->h_error) cudaFreeHost(b->h_error);
+    bfree(b->error);
     b->h_mats = nullptr;
-    b->h_total = b->h_overflow = nullptr;
+    b->h_total = b->h_overflow = b->h_error = nullptr;
     b->ctx = nullptr;
     b->stream = nullptr;
     b->rendered = false;
@@ -482,6 +490,8 @@ sloth_status sloth_batch_create(sloth_ctx *ctx, const sloth_frame_desc *frames, 
     }
     if (cudaMallocHost(&b->h_mats, (ndraws ? ndraws : 1) * sizeof(Mat4)) != cudaSuccess ||
         cudaMallocHost(&b->h_total, 4) != cudaSuccess || cudaMallocHost(&b->h_overflow, 4) != cudaSuccess ||
+        cudaMallocHost(&b->h_error, 4) != cudaSuccess || cudaMalloc(&b->error, 4) != cudaSuccess ||
+        cudaMemset(b->error, 0, 4) != cudaSuccess ||
         prepare_batch_kernels() != cudaSuccess) {
         sloth_batch_detach(b);
         delete b;

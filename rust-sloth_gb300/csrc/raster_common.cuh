@@ -32,7 +32,9 @@ constexpr int kRasterMinBlocks = 5;   // resident CTAs per SM the register budge
 
 template <int TW, int TH>
 struct TileSmem {
-    unsigned long long keys[TH * TW];
+    alignas(128) unsigned long long keys[TH * TW];   // bulk-copy target: 16-byte aligned rows
+    unsigned long long kbar;                          // mbarrier of the tile load
+    uint32_t kok;                                     // the tile load arrived
     unsigned long long ent[kSortCap];
     uint32_t bcount[kDepthBuckets];     // entries per depth bucket, then the scatter cursors
     uint32_t bstart[kDepthBuckets + 1]; // first entry of each bucket (exclusive scan)
@@ -41,6 +43,67 @@ struct TileSmem {
     uint32_t next, zmax_u, zmax_w;
     uint32_t frags[kRasterThreads / 32];
 };
+
+// ---- bulk copies of the key tile (cp.async.bulk, completion on an mbarrier) ----
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Waits at most `limit` polls for phase `parity` of the barrier; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity, uint32_t limit)
+{
+    const uint32_t a = smem_u32(bar);
+    for (uint32_t i = 0; i < limit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_load(void *sdst, const void *gsrc, uint32_t bytes, unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(sdst)),
+                 "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_store(void *gdst, const void *ssrc, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(smem_u32(ssrc)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// Waits until every bulk store of the thread has completed (writes done, smem free).
+__device__ __forceinline__ void bulk_store_drain()
+{
+    asm volatile("cp.async.bulk.commit_group;\ncp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// Orders this thread's generic-proxy shared-memory writes before later async-proxy
+// (bulk copy) accesses.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+constexpr uint32_t kWaitPolls = 1u << 22;   // polls of a bulk-copy barrier before giving up
 
 __device__ __forceinline__ TriRecord load_record(const TriRecord *__restrict__ recs, uint32_t i)
 {
@@ -178,9 +241,30 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
     const int R0 = tr * TH, C0 = tc * TW;
     const bool merge = !split && fb.tile_gen[tile] == fb.gen;
     unsigned long long *gk = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)R0 * g.pitch + C0;
-    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
-        const int rr = i / TW, cc = i - rr * TW;
-        S.keys[i] = merge ? gk[(size_t)rr * g.pitch + cc] : kEmptyKey;
+    if (merge) {
+        // keys of earlier draws since the clear: one bulk copy per tile row (TW*8 bytes,
+        // 16-byte aligned at both ends), completing on an mbarrier
+        if (threadIdx.x < 32) {
+            // warp 0: lane 0 arms the barrier, then the lanes issue one row each
+            if (threadIdx.x == 0) {
+                mbar_init(&S.kbar, 1);
+                fence_proxy_async_smem();
+                mbar_expect_tx(&S.kbar, (uint32_t)(TH * TW * sizeof(unsigned long long)));
+            }
+            __syncwarp();
+            for (int rr = threadIdx.x; rr < TH; rr += 32)
+                bulk_load(&S.keys[rr * TW], gk + (size_t)rr * g.pitch, TW * sizeof(unsigned long long), &S.kbar);
+        }
+        block_sync();
+        if (threadIdx.x == 0) S.kok = (mbar_wait(&S.kbar, 0, kWaitPolls) || mbar_wait(&S.kbar, 0, kWaitPolls)) ? 1u : 0u;
+        block_sync();
+        if (!S.kok) {
+            // the copy did not arrive: report it and leave the tile as it is
+            if (threadIdx.x == 0 && fb.error) atomicOr(fb.error, 1u);
+            return;
+        }
+    } else {
+        for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) S.keys[i] = kEmptyKey;
     }
     if (threadIdx.x == 0) S.zmax_u = S.zmax_w = 0xffffffffu;
 
@@ -350,12 +434,21 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
     if (lane == 0) S.frags[threadIdx.x >> 5] = frags;
     __syncwarp();
     block_sync();
-    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
-        const int rr = i / TW, cc = i - rr * TW;
-        if (!split) {
-            gk[(size_t)rr * g.pitch + cc] = S.keys[i];
-        } else if (S.keys[i] != kEmptyKey) {
-            atomicMin(&gk[(size_t)rr * g.pitch + cc], S.keys[i]);
+    if (!split) {
+        // the tile's keys out: one bulk copy per row, issued once every thread's shared
+        // writes are ordered before the async proxy
+        fence_proxy_async_smem();
+        block_sync();
+        if (threadIdx.x < 32) {
+            // warp 0: one row per lane, each lane waits for its own copies
+            for (int rr = threadIdx.x; rr < TH; rr += 32)
+                bulk_store(gk + (size_t)rr * g.pitch, &S.keys[rr * TW], TW * sizeof(unsigned long long));
+            bulk_store_drain();
+        }
+    } else {
+        for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+            const int rr = i / TW, cc = i - rr * TW;
+            if (S.keys[i] != kEmptyKey) atomicMin(&gk[(size_t)rr * g.pitch + cc], S.keys[i]);
         }
     }
     if (threadIdx.x < 32) {

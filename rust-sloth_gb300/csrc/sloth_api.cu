@@ -73,6 +73,7 @@ struct sloth_ctx {
     size_t tv_cap = 0;
     uint32_t *h_total = nullptr;   // pinned
     unsigned long long *h_frags = nullptr;   // pinned
+    uint32_t *h_error = nullptr;   // pinned copy of fb.error
     uint32_t tri_base = 0;
     bool dirty = true;
 
@@ -239,6 +240,22 @@ static sloth_status ensure_scratch(sloth_ctx *ctx, T **p, size_t *cap, size_t ne
     return SLOTH_OK;
 }
 
+// The device error word travels with the next synchronising call's copies.
+static sloth_status queue_error_copy(sloth_ctx *ctx)
+{
+    CU(ctx, cudaMemcpyAsync(ctx->h_error, ctx->fb.error, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    return SLOTH_OK;
+}
+
+// After a stream synchronisation that followed queue_error_copy.
+static sloth_status report_device_error(sloth_ctx *ctx)
+{
+    if (*ctx->h_error)
+        return fail(ctx, SLOTH_ERR_DEVICE_FAULT, "a raster block gave up waiting for its tile copy (code %u)",
+                    *ctx->h_error);
+    return SLOTH_OK;
+}
+
 static sloth_status resolve_pending(sloth_ctx *ctx)
 {
     if (!ctx->have_frame)
@@ -374,11 +391,19 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
         ctx->own_stream = true;
     }
     if (cudaMallocHost(&ctx->h_total, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMallocHost(&ctx->h_frags, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaMallocHost(&ctx->h_frags, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_error, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&ctx->fb.error, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemset(ctx->fb.error, 0, sizeof(uint32_t)) != cudaSuccess) {
+        if (ctx->h_total) cudaFreeHost(ctx->h_total);
+        if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
+        if (ctx->h_error) cudaFreeHost(ctx->h_error);
+        if (ctx->fb.error) cudaFree(ctx->fb.error);
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         return SLOTH_ERR_OUT_OF_MEMORY;
     }
+    *ctx->h_error = 0;
     *out = ctx;
     return SLOTH_OK;
 }
@@ -406,6 +431,8 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     dfree(ctx->tv);
     if (ctx->h_total) cudaFreeHost(ctx->h_total);
     if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
+    if (ctx->h_error) cudaFreeHost(ctx->h_error);
+    dfree(ctx->fb.error);
     flush_release(ctx->flush);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -494,8 +521,9 @@ sloth_status sloth_ctx_read(sloth_ctx *ctx, uint32_t *cells, float *z, int32_t *
     if (winner)
         CU(ctx, cudaMemcpyAsync(winner, ctx->fb.winner_out, nz * sizeof(int32_t),
                                 cudaMemcpyDeviceToHost, ctx->stream));
+    if ((st = queue_error_copy(ctx)) != SLOTH_OK) return st;
     CU(ctx, cudaStreamSynchronize(ctx->stream));
-    return SLOTH_OK;
+    return report_device_error(ctx);
 }
 
 static sloth_status ctx_flush(sloth_ctx *ctx, int format, uint64_t *bytes)
@@ -507,10 +535,11 @@ static sloth_status ctx_flush(sloth_ctx *ctx, int format, uint64_t *bytes)
     if (st != SLOTH_OK) return st;
     const uint64_t nz = (uint64_t)ctx->g.w * ctx->g.h;
     const uint64_t ncells = ctx->g.image ? nz + ctx->g.h : nz;
+    if ((st = queue_error_copy(ctx)) != SLOTH_OK) return st;
     CU(ctx, timed(ctx, "flush", [&] {
         return flush_run(ctx->flush, ctx->fb.cells_out, ncells, ctx->g.image, format, ctx->stream, bytes);
     }));
-    return SLOTH_OK;
+    return report_device_error(ctx);
 }
 
 sloth_status sloth_ctx_flush(sloth_ctx *ctx, int format, char *out, uint64_t capacity, uint64_t *bytes)
@@ -550,15 +579,17 @@ sloth_status sloth_ctx_read_async(sloth_ctx *ctx, uint32_t *cells, float *z, int
     if (winner)
         CU(ctx, cudaMemcpyAsync(winner, ctx->fb.winner_out, nz * sizeof(int32_t), cudaMemcpyDeviceToHost,
                                 ctx->stream));
-    return SLOTH_OK;
+    return queue_error_copy(ctx);
 }
 
 sloth_status sloth_ctx_synchronize(sloth_ctx *ctx)
 {
     if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
     CU(ctx, cudaSetDevice(ctx->device));
+    sloth_status st = queue_error_copy(ctx);
+    if (st != SLOTH_OK) return st;
     CU(ctx, cudaStreamSynchronize(ctx->stream));
-    return SLOTH_OK;
+    return report_device_error(ctx);
 }
 
 sloth_status sloth_ctx_device_buffers(sloth_ctx *ctx, const uint32_t **cells, const float **z)
@@ -582,9 +613,11 @@ sloth_status sloth_ctx_fragments(sloth_ctx *ctx, uint64_t *fragments)
     CU(ctx, cudaSetDevice(ctx->device));
     CU(ctx, cudaMemcpyAsync(ctx->h_frags, ctx->fb.fragments, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, ctx->stream));
+    sloth_status st = queue_error_copy(ctx);
+    if (st != SLOTH_OK) return st;
     CU(ctx, cudaStreamSynchronize(ctx->stream));
     *fragments = *ctx->h_frags;
-    return SLOTH_OK;
+    return report_device_error(ctx);
 }
 
 // ---------------------------------------------------------------------------------------

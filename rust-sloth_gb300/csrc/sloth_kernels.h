@@ -29,6 +29,7 @@ struct FrameBuffers {
     uint32_t *cells_out;     // w*h (+h)
     int32_t *winner_out;     // w*h
     unsigned long long *fragments;   // covered-sample counter
+    uint32_t *error;         // nonzero once a kernel gave up waiting for its copies (sticky)
     uint32_t gen;            // current clear generation (never 0)
 };
 
