@@ -164,6 +164,12 @@ sloth_status sloth_ctx_flush_device(sloth_ctx *ctx, int format, const char **dev
 /* SLOTH_OPTION_TILE_SHAPE: index of the raster's tile shape (see sloth_tile_shape; 0 is
  *   64 cells x 32 rows); takes effect at the next sloth_ctx_clear. */
 #define SLOTH_OPTION_TILE_SHAPE 2
+/* SLOTH_OPTION_WAIT_TEST: a test hook.  1 makes every raster block that loads keys of an
+ *   earlier draw wait, with a short limit, for 16 bytes that never arrive; the block gives
+ *   up, leaves its tile as it is and the next synchronising call returns
+ *   SLOTH_ERR_DEVICE_FAULT (a clear starts the next frame without the error).  0 (the
+ *   default) is normal operation. */
+#define SLOTH_OPTION_WAIT_TEST 3
 sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value);
 
 /* The raster tile shapes the library is built for: shape i is `cells` depth cells wide

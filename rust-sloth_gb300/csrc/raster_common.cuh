@@ -104,6 +104,7 @@ __device__ __forceinline__ void fence_proxy_async_smem()
 }
 
 constexpr uint32_t kWaitPolls = 1u << 22;   // polls of a bulk-copy barrier before giving up
+constexpr uint32_t kTestWaitPolls = 1u << 10;   // the same under the wait test hook
 
 __device__ __forceinline__ TriRecord load_record(const TriRecord *__restrict__ recs, uint32_t i)
 {
@@ -249,14 +250,17 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
             if (threadIdx.x == 0) {
                 mbar_init(&S.kbar, 1);
                 fence_proxy_async_smem();
-                mbar_expect_tx(&S.kbar, (uint32_t)(TH * TW * sizeof(unsigned long long)));
+                mbar_expect_tx(&S.kbar, (uint32_t)(TH * TW * sizeof(unsigned long long)) + (fb.wait_test ? 16u : 0u));
             }
             __syncwarp();
             for (int rr = threadIdx.x; rr < TH; rr += 32)
                 bulk_load(&S.keys[rr * TW], gk + (size_t)rr * g.pitch, TW * sizeof(unsigned long long), &S.kbar);
         }
         block_sync();
-        if (threadIdx.x == 0) S.kok = (mbar_wait(&S.kbar, 0, kWaitPolls) || mbar_wait(&S.kbar, 0, kWaitPolls)) ? 1u : 0u;
+        if (threadIdx.x == 0) {
+            const uint32_t polls = fb.wait_test ? kTestWaitPolls : kWaitPolls;
+            S.kok = (mbar_wait(&S.kbar, 0, polls) || mbar_wait(&S.kbar, 0, polls)) ? 1u : 0u;
+        }
         block_sync();
         if (!S.kok) {
             // the copy did not arrive: report it and leave the tile as it is

@@ -483,6 +483,8 @@ sloth_status sloth_ctx_clear(sloth_ctx *ctx)
         sloth_status st = alloc_frame(ctx);
         if (st != SLOTH_OK) return st;
     }
+    // A new frame starts without a device error.
+    CU(ctx, cudaMemsetAsync(ctx->fb.error, 0, sizeof(uint32_t), ctx->stream));
     // A new generation invalidates every tile's keys without touching them.
     ctx->fb.gen++;
     if (ctx->fb.gen == 0) {
@@ -784,6 +786,10 @@ sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value)
     case SLOTH_OPTION_TILE_SHAPE:
         if (value < 0 || value >= kNumTileShapes) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "no tile shape %lld", (long long)value);
         ctx->tile_shape = (int)value;
+        return SLOTH_OK;
+    case SLOTH_OPTION_WAIT_TEST:
+        if (value != 0 && value != 1) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "wait test is 0 or 1");
+        ctx->fb.wait_test = (uint32_t)value;
         return SLOTH_OK;
     case SLOTH_OPTION_DEPTH_CULL:
         if (value != 0 && value != 1) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "depth cull is 0 or 1");

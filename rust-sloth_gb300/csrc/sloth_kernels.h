@@ -29,8 +29,9 @@ struct FrameBuffers {
     uint32_t *cells_out;     // w*h (+h)
     int32_t *winner_out;     // w*h
     unsigned long long *fragments;   // covered-sample counter
-    uint32_t *error;         // nonzero once a kernel gave up waiting for its copies (sticky)
+    uint32_t *error;         // nonzero once a kernel gave up waiting for its copies (until the next clear)
     uint32_t gen;            // current clear generation (never 0)
+    uint32_t wait_test;      // test hook: tile loads wait for 16 bytes that never come, briefly
 };
 
 // Binning scratch of one draw.

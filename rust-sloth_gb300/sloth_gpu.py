@@ -23,6 +23,7 @@ OK = 0
 ERR_INVALID_ARGUMENT, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_LIMIT, ERR_DEVICE_FAULT = 1, 2, 3, 4, 5
 OPTION_DEPTH_CULL = 1
 OPTION_TILE_SHAPE = 2
+OPTION_WAIT_TEST = 3
 STATUS ={0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "LIMIT", 5: "DEVICE_FAULT"}
 
 # Every symbol declared in include/sloth_gpu.h, with (restype, argtypes).

@@ -221,3 +221,31 @@ def test_dense_small_viewport_split_tiles(ctx):
     for w, h, image in ((80, 24, True), (81, 23, False)):
         ref = oracle_render([a, b], R, w, h, image)
         assert_same(gpu_render(ctx, [a, b], R, w, h, image), ref, f"dense {w}x{h}")
+
+
+def test_bounded_wait_reports_device_fault(ctx):
+    """SLOTH_OPTION_WAIT_TEST makes every raster block that loads an earlier draw's keys
+    wait for 16 bytes that never come: the blocks give up after a short limit, the read
+    returns SLOTH_ERR_DEVICE_FAULT, and the next frame (after a clear) is exact again."""
+    a, b = W.soup(2000, seed=61, n_large=2), W.soup(2000, seed=62, n_large=2)
+    R = O.euler_rotation(*W.cli_rotation(yaw=0.3))
+    w, h = 80, 40
+    dev = [S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"], None, m["bbox_max"]) for m in (a, b)]
+    ctx.set_viewport(w, h, True)
+    ctx.update(dev)
+    ctx.lib.sloth_ctx_set_option(ctx.h, S.OPTION_WAIT_TEST, 1)
+    ctx.clear()
+    for d in dev:
+        ctx.draw_mesh(d, R)     # the second draw loads the first draw's keys
+    with pytest.raises(S.SlothError) as err:
+        ctx.read()
+    assert err.value.status == S.ERR_DEVICE_FAULT
+    ctx.lib.sloth_ctx_set_option(ctx.h, S.OPTION_WAIT_TEST, 0)
+    ctx.clear()
+    for d in dev:
+        ctx.draw_mesh(d, R)
+    cells, z, winner = ctx.read()
+    ref = oracle_render([a, b], R, w, h, True)
+    assert np.array_equal(cells, ref.cells) and np.array_equal(winner, ref.winner)
+    for d in dev:
+        d.close()
