@@ -128,12 +128,13 @@ __global__ void __launch_bounds__(256) batch_bin_large_kernel(BatchDev b)
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nq = *b.bb.large_count;
-    for (uint32_t q = warp; q < nq; q += nwarps) {
+    const uint32_t items = *b.bb.large_count * kLargeParts;
+    for (uint32_t it = warp; it < items; it += nwarps) {
+        const uint32_t q = it / kLargeParts;
         const BatchFrame &f = b.frames[b.large_frame[q]];
         const uint32_t gtri = b.bb.large_queue[q];
         bin_large_warp<kFill>(f.fb.records[gtri], gtri, vp_batch(f.g), b.bb.tile_count + f.tile_off,
-                              b.bb.tile_cursor + f.tile_off, b.bb.entries, b.bb.capacity, lane);
+                              b.bb.tile_cursor + f.tile_off, b.bb.entries, b.bb.capacity, lane, it % kLargeParts);
     }
 }
 
@@ -269,8 +270,8 @@ cudaError_t launch_batch_newline(const BatchDev &b, const int2 *blocks, uint32_t
 
 cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s)
 {
-    if (fill) batch_bin_large_kernel<true><<<2 * 152, 256, 0, s>>>(b);
-    else batch_bin_large_kernel<false><<<2 * 152, 256, 0, s>>>(b);
+    if (fill) batch_bin_large_kernel<true><<<8 * 152, 256, 0, s>>>(b);
+    else batch_bin_large_kernel<false><<<8 * 152, 256, 0, s>>>(b);
     return cudaGetLastError();
 }
 

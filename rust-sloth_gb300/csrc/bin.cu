@@ -22,12 +22,12 @@ bin_large_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nq = *bb.large_count;
+    const uint32_t items = *bb.large_count * kLargeParts;
     const Viewport vp = vp_of(g);
-    for (uint32_t q = warp; q < nq; q += nwarps) {
-        const uint32_t gtri = tri_base + bb.large_queue[q];
+    for (uint32_t it = warp; it < items; it += nwarps) {
+        const uint32_t gtri = tri_base + bb.large_queue[it / kLargeParts];
         bin_large_warp<kFill>(fb.records[gtri], gtri, vp, bb.tile_count, bb.tile_cursor, bb.entries,
-                              bb.capacity, lane);
+                              bb.capacity, lane, it % kLargeParts);
     }
 }
 
@@ -211,7 +211,7 @@ bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, 
 
 static int large_grid()
 {
-    return 2 * 152;   // two CTAs of 8 warps per SM; the warps stride over the queue
+    return 8 * 152;   // up to eight CTAs of 8 warps per SM; the warps stride over the items
 }
 
 cudaError_t launch_bin_count_large(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,

@@ -17,19 +17,24 @@ __device__ __forceinline__ uint64_t entry_key(float zlo, uint32_t gtri, bool wra
     return ((uint64_t)ordered_z(zlo) << 32) | gtri | (wrapped ? 0x80000000u : 0u);
 }
 
-// One warp walks a large triangle's tile rectangles: counts (kFill false) or writes its
-// entries (kFill true), with a per-tile depth bound (tighter than the triangle-wide one).
+// A large triangle's tiles are split among kLargeParts warps (part p takes every
+// kLargeParts-th group of 32 tiles), so that no lane walks hundreds of tiles in a row.
+constexpr uint32_t kLargeParts = 4;
+
+// One warp walks part `part` of a large triangle's tile rectangles: counts (kFill false)
+// or writes its entries (kFill true), with a per-tile depth bound (tighter than the
+// triangle-wide one).
 template <bool kFill>
 __device__ __forceinline__ void bin_large_warp(const TriRecord &r, uint32_t gtri, const Viewport &vp,
                                                uint32_t *tile_count, uint32_t *tile_cursor,
-                                               uint64_t *entries, uint32_t capacity, int lane)
+                                               uint64_t *entries, uint32_t capacity, int lane, uint32_t part)
 {
     const TileSpan sp = tile_span(vp, r);
     const OrientBound ob = orient_bound(r);
     const int nu = (sp.TU.xb - sp.TU.xa) * (sp.TU.yb - sp.TU.ya);
     const int nw = (sp.TW.xb - sp.TW.xa) * (sp.TW.yb - sp.TW.ya);
     const int uw = sp.TU.xb - sp.TU.xa, ww = sp.TW.xb - sp.TW.xa;
-    for (int k = lane; k < nu + nw; k += 32) {
+    for (int k = (int)part * 32 + lane; k < nu + nw; k += 32 * (int)kLargeParts) {
         int tr, tc;
         if (k < nu) {
             tr = sp.TU.ya + k / uw;
