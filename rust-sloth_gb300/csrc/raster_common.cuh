@@ -126,8 +126,11 @@ __device__ __forceinline__ void raster_part(const TriRecord &r, uint32_t gtri, R
     if ((r.flags & kFlagFiniteXY) && !rect_may_cover(r, c)) return;
     const int bw = c.xb - c.xa;
     const int area = bw * (c.yb - c.ya);
-    const int q = 32 / bw, rem = 32 - q * bw;
-    int dx = lane % bw, dy = lane / bw;
+    // floor(n / bw) for n <= 32 from a reciprocal: (n + 0.5) / bw is at least 0.5 / bw
+    // from an integer, far beyond the reciprocal's rounding error
+    const float rbw = __frcp_rn((float)bw);
+    const int q = (int)(32.5f * rbw), rem = 32 - q * bw;
+    int dy = (int)(((float)lane + 0.5f) * rbw), dx = lane - dy * bw;
     for (int k = lane; k < area; k += 32) {
         const int x = c.xa + dx, y = c.ya + dy;
         const float px = (float)x, py = (float)y;
