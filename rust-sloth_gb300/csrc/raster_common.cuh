@@ -218,12 +218,31 @@ __device__ __forceinline__ void tile_zmax(const unsigned long long *skeys, int R
     mu = 0;
     mw = 0;
     const int wpar = g.w & 1;
-    for (int i = lane; i < TH * TW; i += 32) {
-        const int row = i / TW, col = i - row * TW;
-        const int gr = R0 + row, gc = C0 + col;
-        const uint32_t v = (uint32_t)(*(volatile const unsigned long long *)&skeys[i] >> 32);
-        if (gr >= 1 && gr <= g.h - 2 && gc >= 2 && gc <= g.w - 1 && (gc & 1) == 0) mu = max(mu, v);
-        if (gr >= 2 && gr <= g.h - 1 && gc <= g.w - 4 && (gc & 1) == wpar) mw = max(mw, v);
+    if (R0 >= 2 && R0 + TH <= g.h - 1 && C0 >= 2 && C0 + TW <= g.w - 3) {
+        // every cell of the tile is writable: unwrapped samples write the even columns,
+        // wrapped ones the columns of w's parity (C0 is even); 16-byte reads of
+        // (even, odd) cell pairs
+        const uint32_t base = smem_u32(skeys);
+        uint32_t me = 0, mo = 0;
+#pragma unroll 8
+        for (int i = lane; i < TH * TW / 2; i += 32) {
+            uint32_t lo0, hi0, lo1, hi1;
+            asm volatile("ld.volatile.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(lo0), "=r"(hi0), "=r"(lo1), "=r"(hi1)
+                         : "r"(base + 16u * (uint32_t)i));
+            me = max(me, hi0);
+            mo = max(mo, hi1);
+        }
+        mu = me;
+        mw = wpar ? mo : me;
+    } else {
+        for (int i = lane; i < TH * TW; i += 32) {
+            const int row = i / TW, col = i - row * TW;
+            const int gr = R0 + row, gc = C0 + col;
+            const uint32_t v = (uint32_t)(*(volatile const unsigned long long *)&skeys[i] >> 32);
+            if (gr >= 1 && gr <= g.h - 2 && gc >= 2 && gc <= g.w - 1 && (gc & 1) == 0) mu = max(mu, v);
+            if (gr >= 2 && gr <= g.h - 1 && gc <= g.w - 4 && (gc & 1) == wpar) mw = max(mw, v);
+        }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -365,8 +384,8 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         // it).
         uint32_t wb = 0;          // warp-uniform: the bucket of the current window's first entry
         // warp-uniform count of warp walks since the warp's last refresh of the bound: one
-        // refresh per 16 walks of a warp (about one per 16 entries of the CTA, as the
-        // warps take turns), warp w's first after 2 + 2w walks
+        // refresh per 16 walks of a warp (culled entries do not count), warp w's first
+        // after 2 + 2w walks
         uint32_t since = 14u - 2u * (uint32_t)wid;
         for (uint32_t w0 = 0; w0 < n; w0 += kRasterThreads) {
             if (depth_cull) {
@@ -413,7 +432,6 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                         }
                         since = 0;
                     }
-                    ++since;
                     // lane 0 decides for the warp (the bounds may move between reads)
                     const unsigned long long es = __shfl_sync(0xffffffffu, ent, src);
                     uint32_t hidden = 0;
@@ -422,6 +440,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                         hidden = (uint32_t)(es >> 32) > (((uint32_t)es & 0x80000000u) ? max(zu, zw) : zu);
                     }
                     if (__shfl_sync(0xffffffffu, hidden, 0)) continue;
+                    ++since;   // culled entries change no key: only walks count
                 }
                 const uint32_t gt = __shfl_sync(0xffffffffu, gtri, src);
                 const TriRecord r = load_record(fb.records, gt);
