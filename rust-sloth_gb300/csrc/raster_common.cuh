@@ -377,17 +377,24 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         }
         if (threadIdx.x == 0) S.next = 0;
         block_sync();
-        // Windows of kRasterThreads sorted entries; lane i of warp w takes entry w + 8i, so
-        // that the warps move through the sorted order together.  Each lane loads its own
-        // record; a small triangle is walked by its lane, a larger one by the whole warp
-        // (in the warp's sorted order, each checked against the depth bound right before
-        // it).
+        // Windows of kRasterThreads sorted entries, each in 8 interleaved slots: lane i of
+        // slot j takes entry j + 8i, so that a warp's lanes spread over the window and the
+        // warps move through the sorted order together.  The warps claim slots in order
+        // from a shared counter, so that a warp done early takes more.  Each lane loads its
+        // own record; a small triangle is walked by its lane, a larger one by the whole
+        // warp (in the warp's sorted order, checked against the depth bound before each).
+        constexpr uint32_t kSlots = kRasterThreads / 32;
         uint32_t wb = 0;          // warp-uniform: the bucket of the current window's first entry
         // warp-uniform count of warp walks since the warp's last refresh of the bound: one
         // refresh per 16 walks of a warp (culled entries do not count), warp w's first
         // after 2 + 2w walks
         uint32_t since = 14u - 2u * (uint32_t)wid;
-        for (uint32_t w0 = 0; w0 < n; w0 += kRasterThreads) {
+        for (;;) {
+            uint32_t claim = 0;
+            if (lane == 0) claim = atomicAdd(&S.next, 1u);
+            claim = __shfl_sync(0xffffffffu, claim, 0);
+            const uint32_t w0 = (claim / kSlots) * kRasterThreads;
+            if (w0 >= n) break;
             if (depth_cull) {
                 // every entry from here on lies in bucket wb or later: when that bucket's
                 // smallest bound is behind every writable cell, so is everything left
@@ -395,7 +402,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                 const uint32_t zu = *(volatile uint32_t *)&S.zmax_u, zw = *(volatile uint32_t *)&S.zmax_w;
                 if (S.bmin[wb] > max(zu, zw)) break;
             }
-            const uint32_t e = w0 + wid + (kRasterThreads / 32) * lane;
+            const uint32_t e = w0 + claim % kSlots + kSlots * lane;
             const unsigned long long ent = e < n ? S.ent[e] : ~0ull;
             bool live = e < n;
             if (depth_cull && live) {
@@ -420,8 +427,6 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
             }
             unsigned coop = __ballot_sync(0xffffffffu, live && !serial);
             while (coop) {
-                const int src = __ffs(coop) - 1;
-                coop &= coop - 1;
                 if (depth_cull) {
                     if (since >= 16) {
                         uint32_t mu, mw;
@@ -432,16 +437,18 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                         }
                         since = 0;
                     }
-                    // lane 0 decides for the warp (the bounds may move between reads)
-                    const unsigned long long es = __shfl_sync(0xffffffffu, ent, src);
-                    uint32_t hidden = 0;
-                    if (lane == 0) {
-                        const uint32_t zu = *(volatile uint32_t *)&S.zmax_u, zw = *(volatile uint32_t *)&S.zmax_w;
-                        hidden = (uint32_t)(es >> 32) > (((uint32_t)es & 0x80000000u) ? max(zu, zw) : zu);
-                    }
-                    if (__shfl_sync(0xffffffffu, hidden, 0)) continue;
+                    // every lane checks its own waiting entry against the bound; each
+                    // decision stands on its own (the bound only falls), so the lanes may
+                    // read different values
+                    const uint32_t zu = *(volatile uint32_t *)&S.zmax_u, zw = *(volatile uint32_t *)&S.zmax_w;
+                    const bool hidden = ((coop >> lane) & 1u) &&
+                                        (uint32_t)(ent >> 32) > (((uint32_t)ent & 0x80000000u) ? max(zu, zw) : zu);
+                    coop &= ~__ballot_sync(0xffffffffu, hidden);
+                    if (!coop) break;
                     ++since;   // culled entries change no key: only walks count
                 }
+                const int src = __ffs(coop) - 1;
+                coop &= coop - 1;
                 const uint32_t gt = __shfl_sync(0xffffffffu, gtri, src);
                 const TriRecord r = load_record(fb.records, gt);
                 const Rect U = unwrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
