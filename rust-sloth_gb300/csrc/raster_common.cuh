@@ -116,36 +116,105 @@ __device__ __forceinline__ TriRecord load_record(const TriRecord *__restrict__ r
     return r;
 }
 
-// Walk the samples of rect c (row-major, 32 at a time) and fold covered samples' keys.
+// One sample of the reference's loop body: edge test, depth, key folded into the tile.
+template <int TW, int kNotWrapped>
+__device__ __forceinline__ void fold_sample(const TriRecord &r, uint32_t gtri, int x, int y, int R0, int C0,
+                                            int w, unsigned long long *skeys, uint32_t &frags)
+{
+    const EdgeVals e = eval_edges(r, (float)x, (float)y);
+    if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
+        ++frags;
+        const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
+        if (z < kFltMax) {
+            const unsigned long long key = make_key(z, gtri, kNotWrapped);
+            const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
+            const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
+            unsigned long long *p = &skeys[row * TW + col];
+            if (key < *(volatile unsigned long long *)p) atomicMin(p, key);
+        }
+    }
+}
+
+// One edge's columns on one row: for records with kFlagFiniteXY the edge value
+// w(x) = fl(A - fl(dy * fl(x - ax))), A = fl(dx * fl(py - ay)), is monotone in x (a chain of
+// correctly rounded monotone operations, no overflow), so the columns where w >= 0 are a
+// prefix (dy > 0), a suffix (dy < 0) or all or none (dy == 0) of the row.  The real-valued
+// crossing only estimates the end; the exact value at the first column past it decides
+// (stepping on while it still passes), so [lo, hi) keeps every column that passes.
+__device__ __forceinline__ void edge_row_span(float dx, float dy, float ax, float ay, float py, int &lo, int &hi)
+{
+    if (lo >= hi) return;
+    if (dy == 0.0f) {
+        if (!(edge_eval(dx, dy, ax, ay, (float)lo, py) >= 0.0f)) hi = lo;
+        return;
+    }
+    const float cross = ax + __fdividef(fmul(dx, fsub(py, ay)), dy);   // estimate only
+    if (dy > 0.0f) {
+        int t = (int)fminf(fmaxf(floorf(cross), (float)(lo - 1)), (float)(hi - 1)) + 1;
+        while (t < hi && edge_eval(dx, dy, ax, ay, (float)t, py) >= 0.0f) ++t;
+        hi = t;
+    } else {
+        int t = (int)fminf(fmaxf(ceilf(cross), (float)lo), (float)hi) - 1;
+        while (t >= lo && edge_eval(dx, dy, ax, ay, (float)t, py) >= 0.0f) --t;
+        lo = t + 1;
+    }
+}
+
+// Parts of more samples than this are walked over their rows' column spans; smaller ones
+// over the whole rectangle.
+constexpr int kSpanMinSamples = 64;
+
+// Walk the samples of rect c and fold covered samples' keys.  Large parts of records with
+// kFlagFiniteXY: lane i bounds row c.ya + i to the columns that can pass all three edges
+// (at most 32 rows: a part lies in one tile), and the warp walks the concatenated spans
+// 32 samples at a time, each lane finding its row by a binary search over the spans'
+// running ends.  Otherwise the rectangle, row-major, 32 samples at a time.  Every walked
+// sample gets the exact test.
 template <int TW, int kNotWrapped>
 __device__ __forceinline__ void raster_part(const TriRecord &r, uint32_t gtri, Rect c, int R0,
                                             int C0, int w, unsigned long long *skeys, int lane,
                                             uint32_t &frags)
 {
     if (c.empty()) return;
-    if ((r.flags & kFlagFiniteXY) && !rect_may_cover(r, c)) return;
+    const bool finite = (r.flags & kFlagFiniteXY) != 0;
+    if (finite && !rect_may_cover(r, c)) return;
     const int bw = c.xb - c.xa;
     const int area = bw * (c.yb - c.ya);
+    if (finite && area > kSpanMinSamples) {
+        const int y = c.ya + lane;
+        int lo = c.xa, hi = y < c.yb ? c.xb : c.xa;
+        const float py = (float)y;
+        edge_row_span(r.dx0, r.dy0, r.v2x, r.v2y, py, lo, hi);
+        edge_row_span(r.dx1, r.dy1, r.v3x, r.v3y, py, lo, hi);
+        edge_row_span(r.dx2, r.dy2, r.v1x, r.v1y, py, lo, hi);
+        const int len = max(hi - lo, 0);
+        int end = len;   // running end of the spans up to this row
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int o = __shfl_up_sync(0xffffffffu, end, d);
+            if (lane >= d) end += o;
+        }
+        const int total = __shfl_sync(0xffffffffu, end, 31);
+        const int xoff = lo - (end - len);   // column of span sample k of this row: k + xoff
+        for (int base = 0; base < total; base += 32) {
+            const int k = base + lane;
+            // the row of sample k: the number of rows whose spans end at or before k
+            int row = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(0xffffffffu, end, row + step - 1) <= k) row += step;
+            const int x = k + __shfl_sync(0xffffffffu, xoff, row);
+            if (k < total) fold_sample<TW, kNotWrapped>(r, gtri, x, c.ya + row, R0, C0, w, skeys, frags);
+        }
+        return;
+    }
     // floor(n / bw) for n <= 32 from a reciprocal: (n + 0.5) / bw is at least 0.5 / bw
     // from an integer, far beyond the reciprocal's rounding error
     const float rbw = __frcp_rn((float)bw);
     const int q = (int)(32.5f * rbw), rem = 32 - q * bw;
     int dy = (int)(((float)lane + 0.5f) * rbw), dx = lane - dy * bw;
     for (int k = lane; k < area; k += 32) {
-        const int x = c.xa + dx, y = c.ya + dy;
-        const float px = (float)x, py = (float)y;
-        const EdgeVals e = eval_edges(r, px, py);
-        if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
-            ++frags;
-            const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
-            if (z < kFltMax) {
-                const unsigned long long key = make_key(z, gtri, kNotWrapped);
-                const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
-                const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
-                unsigned long long *p = &skeys[row * TW + col];
-                if (key < *(volatile unsigned long long *)p) atomicMin(p, key);
-            }
-        }
+        fold_sample<TW, kNotWrapped>(r, gtri, c.xa + dx, c.ya + dy, R0, C0, w, skeys, frags);
         dx += rem;
         dy += q;
         if (dx >= bw) {
@@ -172,25 +241,6 @@ __device__ __forceinline__ Rect tile_part(const TriRecord &r, const Viewport &vp
 __device__ __forceinline__ int rect_area(const Rect &c)
 {
     return c.empty() ? 0 : (c.xb - c.xa) * (c.yb - c.ya);
-}
-
-// One sample of the reference's loop body: edge test, depth, key folded into the tile.
-template <int TW, int kNotWrapped>
-__device__ __forceinline__ void fold_sample(const TriRecord &r, uint32_t gtri, int x, int y, int R0, int C0,
-                                            int w, unsigned long long *skeys, uint32_t &frags)
-{
-    const EdgeVals e = eval_edges(r, (float)x, (float)y);
-    if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
-        ++frags;
-        const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
-        if (z < kFltMax) {
-            const unsigned long long key = make_key(z, gtri, kNotWrapped);
-            const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
-            const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
-            unsigned long long *p = &skeys[row * TW + col];
-            if (key < *(volatile unsigned long long *)p) atomicMin(p, key);
-        }
-    }
 }
 
 // One lane walks every sample of rect c.
@@ -260,6 +310,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                                             int tile, uint32_t cnt, const uint64_t *__restrict__ entries,
                                             int depth_cull, bool split = false)
 {
+    static_assert(TH <= 32, "a tile part has at most 32 rows: one lane per row in raster_part");
     const int tr = tile / g.ntx, tc = tile - (tile / g.ntx) * g.ntx;
     const int R0 = tr * TH, C0 = tc * TW;
     const bool merge = !split && fb.tile_gen[tile] == fb.gen;
@@ -399,8 +450,10 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                 // every entry from here on lies in bucket wb or later: when that bucket's
                 // smallest bound is behind every writable cell, so is everything left
                 while (S.bstart[wb + 1] <= w0) ++wb;
+                // lane 0 decides for the warp: the bounds may fall between the lanes' reads,
+                // and a warp that left the loop in part would wait on itself
                 const uint32_t zu = *(volatile uint32_t *)&S.zmax_u, zw = *(volatile uint32_t *)&S.zmax_w;
-                if (S.bmin[wb] > max(zu, zw)) break;
+                if (__shfl_sync(0xffffffffu, S.bmin[wb] > max(zu, zw) ? 1u : 0u, 0)) break;
             }
             const uint32_t e = w0 + claim % kSlots + kSlots * lane;
             const unsigned long long ent = e < n ? S.ent[e] : ~0ull;

@@ -127,6 +127,57 @@ def test_scaled_config2_soup(ctx, w, h):
 
 
 
+def span_soup(seed, w, h, n=600):
+    """Screen-space triangles (identity transforms) that stress the per-row column spans
+    of large tile parts: vertices on sample positions (edges through samples, w == 0),
+    horizontal and vertical edges, long thin slivers, half-sample offsets, vertices far
+    off screen and huge finite coordinates; both windings."""
+    rng = np.random.default_rng(seed)
+    xs = w // 2 if w > 0 else 1
+    tris = []
+    for k in range(n):
+        kind = k % 7
+        c = rng.uniform([0, 0], [xs, h])
+        s = rng.uniform(4, 40)
+        if kind == 0:      # integer vertices
+            v = np.round(c + rng.uniform(-s, s, (3, 2)))
+        elif kind == 1:    # right triangle: one horizontal and one vertical edge
+            a, b = np.round(c), np.round(c + rng.uniform(-s, s, 2))
+            v = np.array([a, [b[0], a[1]], [a[0], b[1]]])
+        elif kind == 2:    # long sliver
+            d = rng.normal(size=2)
+            d /= np.linalg.norm(d)
+            v = np.array([c - 3 * s * d, c + 3 * s * d, c + 3 * s * d + rng.uniform(0.05, 1.5) * d[::-1] * [1, -1]])
+        elif kind == 3:    # half-sample offsets
+            v = np.round(c + rng.uniform(-s, s, (3, 2))) + 0.5
+        elif kind == 4:    # vertices far off screen
+            v = c + rng.uniform(-20 * s, 20 * s, (3, 2))
+        elif kind == 5:    # huge finite coordinates on one vertex
+            v = c + rng.uniform(-s, s, (3, 2))
+            v[1] = [rng.choice([-1, 1]) * 10.0 ** rng.uniform(6, 17), c[1] + rng.uniform(-s, s)]
+        else:              # random floats
+            v = c + rng.uniform(-s, s, (3, 2))
+        if rng.random() < 0.5:
+            v = v[::-1]
+        z = rng.uniform(-1, 1, 3)
+        tris.append(np.column_stack([v, z]))
+    t = np.asarray(tris, np.float32).reshape(-1, 3)
+    rgb = rng.integers(0, 256, (n, 3), dtype=np.uint8)
+    return {"x": t[:, 0].copy(), "y": t[:, 1].copy(), "z": t[:, 2].copy(), "idx": None, "rgb": rgb,
+            "bbox_max": np.ones(3, np.float32)}
+
+
+@pytest.mark.parametrize("seed", range(4))
+@pytest.mark.parametrize("image", [True, False])
+def test_row_span_walk(ctx, seed, image):
+    w, h = (403, 150) if seed % 2 else (512, 128)
+    m = span_soup(seed, w if image else 2 * w, h)
+    eye = np.eye(4, dtype=np.float32)
+    ref = oracle_render([m], eye, w, h, image, U=eye)
+    assert ref.fragments > 0
+    assert_same(gpu_render(ctx, [m], eye, w, h, image, U=eye), ref, f"span soup {seed} image={image}")
+
+
 def test_depth_culling_skips_hidden_fragments(ctx):
     """At config 2's triangle size and depth complexity (1/8 of its viewport: 1/64 of the
     triangles, 8x the vertex offsets) the depth culling skips most covered samples and
