@@ -41,6 +41,7 @@ struct TileSmem {
     uint32_t bmin[kDepthBuckets];       // smallest depth bound in each bucket
     uint32_t zlo_min, zlo_max;
     uint32_t next, zmax_u, zmax_w;
+    uint32_t rmu[32], rmw[32];          // the same bounds per row of the tile
     uint32_t frags[kRasterThreads / 32];
 };
 
@@ -166,14 +167,16 @@ constexpr int kSpanMinSamples = 64;
 
 // Walk the samples of rect c and fold covered samples' keys.  Large parts of records with
 // kFlagFiniteXY: lane i bounds row c.ya + i to the columns that can pass all three edges
-// (at most 32 rows: a part lies in one tile), and the warp walks the concatenated spans
+// (at most 32 rows: a part lies in one tile) -- none when the row's depth bound (rowmax,
+// indexed by tile row) is below the entry's depth bound zb -- and the warp walks the
+// concatenated spans
 // 32 samples at a time, each lane finding its row by a binary search over the spans'
 // running ends.  Otherwise the rectangle, row-major, 32 samples at a time.  Every walked
 // sample gets the exact test.
 template <int TW, int kNotWrapped>
 __device__ __forceinline__ void raster_part(const TriRecord &r, uint32_t gtri, Rect c, int R0,
                                             int C0, int w, unsigned long long *skeys, int lane,
-                                            uint32_t &frags)
+                                            uint32_t &frags, const uint32_t *rowmax, uint32_t zb)
 {
     if (c.empty()) return;
     const bool finite = (r.flags & kFlagFiniteXY) != 0;
@@ -183,6 +186,8 @@ __device__ __forceinline__ void raster_part(const TriRecord &r, uint32_t gtri, R
     if (finite && area > kSpanMinSamples) {
         const int y = c.ya + lane;
         int lo = c.xa, hi = y < c.yb ? c.xb : c.xa;
+        // a row whose every writable cell is nearer than the entry's depth bound is done
+        if (hi > lo && zb > *(volatile const uint32_t *)&rowmax[kNotWrapped ? y - R0 : y + 1 - R0]) hi = lo;
         const float py = (float)y;
         edge_row_span(r.dx0, r.dy0, r.v2x, r.v2y, py, lo, hi);
         edge_row_span(r.dx1, r.dy1, r.v3x, r.v3y, py, lo, hi);
@@ -256,48 +261,60 @@ __device__ __forceinline__ void raster_serial(const TriRecord &r, uint32_t gtri,
 // lane alone; larger ones by the whole warp.
 constexpr int kSerialMaxSamples = 16;
 
-// Upper bounds of the farthest depth (ordered high key word) among the tile's cells that
-// unwrapped samples can write (row y in [1,h-2], column 2x in [2,w-1], even) and among
-// those wrapped samples can write (row y+1 in [2,h-1], column 2x-w in [0,w-4], of the
-// parity of w).  Reads race with the atomics of other warps; key values only decrease, so
-// the results stay upper bounds of every later state.
+// Depth bounds: zmax_u / zmax_w are upper bounds of the farthest depth (ordered high key
+// word) among the tile's cells that unwrapped samples can write (row y in [1,h-2], column
+// 2x in [2,w-1], even) and among those wrapped samples can write (row y+1 in [2,h-1],
+// column 2x-w in [0,w-4], of the parity of w); rmu[i] / rmw[i] are the same over tile row
+// i.  Lane i of the refreshing warp reads row i (16-byte reads of (even, odd) cell pairs,
+// rotated by lane so that the lanes of a read hit different banks) and folds its maxima in
+// with atomicMin.  Reads race with the atomics of other warps; key values only decrease,
+// so every bound read stays an upper bound of every later state.
 template <int TW, int TH>
-__device__ __forceinline__ void tile_zmax(const unsigned long long *skeys, int R0, int C0,
-                                          const FrameGeom &g, int lane, uint32_t &mu, uint32_t &mw)
+__device__ __forceinline__ void refresh_bounds(TileSmem<TW, TH> &S, int R0, int C0, const FrameGeom &g, int lane)
 {
-    mu = 0;
-    mw = 0;
+    constexpr int P = TW / 2;   // cell pairs per row
+    static_assert((P & (P - 1)) == 0, "rotation by mask");
     const int wpar = g.w & 1;
-    if (R0 >= 2 && R0 + TH <= g.h - 1 && C0 >= 2 && C0 + TW <= g.w - 3) {
-        // every cell of the tile is writable: unwrapped samples write the even columns,
-        // wrapped ones the columns of w's parity (C0 is even); 16-byte reads of
-        // (even, odd) cell pairs
-        const uint32_t base = smem_u32(skeys);
-        uint32_t me = 0, mo = 0;
+    uint32_t mu = 0, mw = 0;
+    if (lane < TH) {
+        const uint32_t base = smem_u32(S.keys) + 8u * (uint32_t)(lane * TW);
+        if (R0 >= 2 && R0 + TH <= g.h - 1 && C0 >= 2 && C0 + TW <= g.w - 3) {
+            // every cell of the tile is writable: unwrapped samples write the even columns,
+            // wrapped ones the columns of w's parity (C0 is even)
 #pragma unroll 8
-        for (int i = lane; i < TH * TW / 2; i += 32) {
-            uint32_t lo0, hi0, lo1, hi1;
-            asm volatile("ld.volatile.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
-                         : "=r"(lo0), "=r"(hi0), "=r"(lo1), "=r"(hi1)
-                         : "r"(base + 16u * (uint32_t)i));
-            me = max(me, hi0);
-            mo = max(mo, hi1);
+            for (int k = 0; k < P; ++k) {
+                uint32_t lo0, hi0, lo1, hi1;
+                asm volatile("ld.volatile.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                             : "=r"(lo0), "=r"(hi0), "=r"(lo1), "=r"(hi1)
+                             : "r"(base + 16u * (uint32_t)((k + lane) & (P - 1))));
+                mu = max(mu, hi0);
+                mw = max(mw, wpar ? hi1 : hi0);
+            }
+        } else {
+            const int gr = R0 + lane;
+            const bool ru = gr >= 1 && gr <= g.h - 2, rw = gr >= 2 && gr <= g.h - 1;
+            for (int k = 0; k < P; ++k) {
+                const int pi = (k + lane) & (P - 1);
+                uint32_t lo0, hi0, lo1, hi1;
+                asm volatile("ld.volatile.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                             : "=r"(lo0), "=r"(hi0), "=r"(lo1), "=r"(hi1)
+                             : "r"(base + 16u * (uint32_t)pi));
+                const int gc = C0 + 2 * pi;   // even
+                if (ru && gc >= 2 && gc <= g.w - 1) mu = max(mu, hi0);
+                if (rw && gc + wpar <= g.w - 4) mw = max(mw, wpar ? hi1 : hi0);
+            }
         }
-        mu = me;
-        mw = wpar ? mo : me;
-    } else {
-        for (int i = lane; i < TH * TW; i += 32) {
-            const int row = i / TW, col = i - row * TW;
-            const int gr = R0 + row, gc = C0 + col;
-            const uint32_t v = (uint32_t)(*(volatile const unsigned long long *)&skeys[i] >> 32);
-            if (gr >= 1 && gr <= g.h - 2 && gc >= 2 && gc <= g.w - 1 && (gc & 1) == 0) mu = max(mu, v);
-            if (gr >= 2 && gr <= g.h - 1 && gc <= g.w - 4 && (gc & 1) == wpar) mw = max(mw, v);
-        }
+        atomicMin(&S.rmu[lane], mu);
+        atomicMin(&S.rmw[lane], mw);
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
         mu = max(mu, __shfl_xor_sync(0xffffffffu, mu, d));
         mw = max(mw, __shfl_xor_sync(0xffffffffu, mw, d));
+    }
+    if (lane == 0) {
+        atomicMin(&S.zmax_u, mu);
+        atomicMin(&S.zmax_w, mw);
     }
 }
 
@@ -344,6 +361,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) S.keys[i] = kEmptyKey;
     }
     if (threadIdx.x == 0) S.zmax_u = S.zmax_w = 0xffffffffu;
+    if (threadIdx.x < 64) (threadIdx.x < 32 ? S.rmu : S.rmw)[threadIdx.x & 31] = 0xffffffffu;
 
     const int lane = threadIdx.x & 31;
     const Viewport vp{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
@@ -482,12 +500,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
             while (coop) {
                 if (depth_cull) {
                     if (since >= 16) {
-                        uint32_t mu, mw;
-                        tile_zmax<TW, TH>(S.keys, R0, C0, g, lane, mu, mw);
-                        if (lane == 0) {
-                            atomicMin(&S.zmax_u, mu);
-                            atomicMin(&S.zmax_w, mw);
-                        }
+                        refresh_bounds<TW, TH>(S, R0, C0, g, lane);
                         since = 0;
                     }
                     // every lane checks its own waiting entry against the bound; each
@@ -503,13 +516,16 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                 const int src = __ffs(coop) - 1;
                 coop &= coop - 1;
                 const uint32_t gt = __shfl_sync(0xffffffffu, gtri, src);
+                const uint32_t zb = depth_cull ? __shfl_sync(0xffffffffu, (uint32_t)(ent >> 32), src) : 0u;
                 const TriRecord r = load_record(fb.records, gt);
                 const Rect U = unwrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
                 if (!U.empty())
-                    raster_part<TW, 1>(r, gt, clip_unwrapped(vp, U, tr, tc), R0, C0, g.w, S.keys, lane, frags);
+                    raster_part<TW, 1>(r, gt, clip_unwrapped(vp, U, tr, tc), R0, C0, g.w, S.keys, lane, frags,
+                                       S.rmu, zb);
                 const Rect W = wrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
                 if (!W.empty())
-                    raster_part<TW, 0>(r, gt, clip_wrapped(vp, W, tr, tc), R0, C0, g.w, S.keys, lane, frags);
+                    raster_part<TW, 0>(r, gt, clip_wrapped(vp, W, tr, tc), R0, C0, g.w, S.keys, lane, frags,
+                                       S.rmw, zb);
             }
         }
         block_sync();
