@@ -118,19 +118,22 @@ __device__ __forceinline__ TriRecord load_record(const TriRecord *__restrict__ r
 }
 
 // One sample of the reference's loop body: edge test, depth, key folded into the tile.
+// With a depth bound zb of the triangle in this tile (0: none), a cell already nearer
+// than zb is passed over before the edge test: no depth of the triangle can beat it.
 template <int TW, int kNotWrapped>
 __device__ __forceinline__ void fold_sample(const TriRecord &r, uint32_t gtri, int x, int y, int R0, int C0,
-                                            int w, unsigned long long *skeys, uint32_t &frags)
+                                            int w, unsigned long long *skeys, uint32_t &frags, uint32_t zb)
 {
+    const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
+    const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
+    unsigned long long *p = &skeys[row * TW + col];
+    if (zb > *(volatile const uint32_t *)(reinterpret_cast<const uint32_t *>(p) + 1)) return;
     const EdgeVals e = eval_edges(r, (float)x, (float)y);
     if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
         ++frags;
         const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
         if (z < kFltMax) {
             const unsigned long long key = make_key(z, gtri, kNotWrapped);
-            const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
-            const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
-            unsigned long long *p = &skeys[row * TW + col];
             if (key < *(volatile unsigned long long *)p) atomicMin(p, key);
         }
     }
@@ -209,7 +212,7 @@ __device__ __forceinline__ void raster_part(const TriRecord &r, uint32_t gtri, R
             for (int step = 16; step > 0; step >>= 1)
                 if (__shfl_sync(0xffffffffu, end, row + step - 1) <= k) row += step;
             const int x = k + __shfl_sync(0xffffffffu, xoff, row);
-            if (k < total) fold_sample<TW, kNotWrapped>(r, gtri, x, c.ya + row, R0, C0, w, skeys, frags);
+            if (k < total) fold_sample<TW, kNotWrapped>(r, gtri, x, c.ya + row, R0, C0, w, skeys, frags, zb);
         }
         return;
     }
@@ -219,7 +222,7 @@ __device__ __forceinline__ void raster_part(const TriRecord &r, uint32_t gtri, R
     const int q = (int)(32.5f * rbw), rem = 32 - q * bw;
     int dy = (int)(((float)lane + 0.5f) * rbw), dx = lane - dy * bw;
     for (int k = lane; k < area; k += 32) {
-        fold_sample<TW, kNotWrapped>(r, gtri, c.xa + dx, c.ya + dy, R0, C0, w, skeys, frags);
+        fold_sample<TW, kNotWrapped>(r, gtri, c.xa + dx, c.ya + dy, R0, C0, w, skeys, frags, zb);
         dx += rem;
         dy += q;
         if (dx >= bw) {
@@ -251,10 +254,10 @@ __device__ __forceinline__ int rect_area(const Rect &c)
 // One lane walks every sample of rect c.
 template <int TW, int kNotWrapped>
 __device__ __forceinline__ void raster_serial(const TriRecord &r, uint32_t gtri, const Rect &c, int R0, int C0,
-                                              int w, unsigned long long *skeys, uint32_t &frags)
+                                              int w, unsigned long long *skeys, uint32_t &frags, uint32_t zb)
 {
     for (int y = c.ya; y < c.yb; ++y)
-        for (int x = c.xa; x < c.xb; ++x) fold_sample<TW, kNotWrapped>(r, gtri, x, y, R0, C0, w, skeys, frags);
+        for (int x = c.xa; x < c.xb; ++x) fold_sample<TW, kNotWrapped>(r, gtri, x, y, R0, C0, w, skeys, frags, zb);
 }
 
 // Entries whose clipped rectangles hold at most this many samples are walked by their
@@ -493,8 +496,9 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
             const bool serial = live && area <= kSerialMaxSamples;
             if (serial) {
                 const TriRecord r = load_record(fb.records, gtri);
-                raster_serial<TW, 1>(r, gtri, tile_part<1>(r, vp, tr, tc), R0, C0, g.w, S.keys, frags);
-                raster_serial<TW, 0>(r, gtri, tile_part<0>(r, vp, tr, tc), R0, C0, g.w, S.keys, frags);
+                const uint32_t zb = depth_cull ? (uint32_t)(ent >> 32) : 0u;
+                raster_serial<TW, 1>(r, gtri, tile_part<1>(r, vp, tr, tc), R0, C0, g.w, S.keys, frags, zb);
+                raster_serial<TW, 0>(r, gtri, tile_part<0>(r, vp, tr, tc), R0, C0, g.w, S.keys, frags, zb);
             }
             unsigned coop = __ballot_sync(0xffffffffu, live && !serial);
             while (coop) {
