@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) batch_bin_large_kernel(BatchDev b)
         const uint32_t q = it / kLargeParts;
         const BatchFrame &f = b.frames[b.large_frame[q]];
         const uint32_t gtri = b.bb.large_queue[q];
-        bin_large_warp<kFill>(f.fb.records[gtri], gtri, vp_batch(f.g), b.bb.tile_count + f.tile_off,
+        bin_large_warp<kFill>(f.fb.records + gtri, gtri, vp_batch(f.g), b.bb.tile_count + f.tile_off,
                               b.bb.tile_cursor + f.tile_off, b.bb.entries, b.bb.capacity, lane, it % kLargeParts);
     }
 }

@@ -26,7 +26,7 @@ bin_large_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
     const Viewport vp = vp_of(g);
     for (uint32_t it = warp; it < items; it += nwarps) {
         const uint32_t gtri = tri_base + bb.large_queue[it / kLargeParts];
-        bin_large_warp<kFill>(fb.records[gtri], gtri, vp, bb.tile_count, bb.tile_cursor, bb.entries,
+        bin_large_warp<kFill>(fb.records + gtri, gtri, vp, bb.tile_count, bb.tile_cursor, bb.entries,
                               bb.capacity, lane, it % kLargeParts);
     }
 }

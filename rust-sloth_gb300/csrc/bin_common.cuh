@@ -24,16 +24,21 @@ constexpr uint32_t kLargeParts = 4;
 // One warp walks part `part` of a large triangle's tile rectangles: counts (kFill false)
 // or writes its entries (kFill true), with a per-tile depth bound (tighter than the
 // triangle-wide one).
+// The sample range (16 bytes) decides first whether the part has tiles at all; only then
+// is the whole record read.
 template <bool kFill>
-__device__ __forceinline__ void bin_large_warp(const TriRecord &r, uint32_t gtri, const Viewport &vp,
+__device__ __forceinline__ void bin_large_warp(const TriRecord *rec, uint32_t gtri, const Viewport &vp,
                                                uint32_t *tile_count, uint32_t *tile_cursor,
                                                uint64_t *entries, uint32_t capacity, int lane, uint32_t part)
 {
-    const TileSpan sp = tile_span(vp, r);
-    const OrientBound ob = orient_bound(r);
+    const int4 xr = __ldg(reinterpret_cast<const int4 *>(rec) + 4);
+    const TileSpan sp = tile_span_of(vp, xr.x, xr.y, xr.z, xr.w);
     const int nu = (sp.TU.xb - sp.TU.xa) * (sp.TU.yb - sp.TU.ya);
     const int nw = (sp.TW.xb - sp.TW.xa) * (sp.TW.yb - sp.TW.ya);
     const int uw = sp.TU.xb - sp.TU.xa, ww = sp.TW.xb - sp.TW.xa;
+    if ((int)part * 32 >= nu + nw) return;
+    const TriRecord r = *rec;
+    const OrientBound ob = orient_bound(r);
     for (int k = (int)part * 32 + lane; k < nu + nw; k += 32 * (int)kLargeParts) {
         int tr, tc;
         if (k < nu) {

@@ -223,14 +223,14 @@ struct TileSpan {
     uint32_t ntiles;    // tiles of both rectangles (an upper bound of the tiles hit)
     bool large;         // binned by a warp instead of a thread
 };
-__device__ __forceinline__ TileSpan tile_span(const Viewport &vp, const TriRecord &r)
+__device__ __forceinline__ TileSpan tile_span_of(const Viewport &vp, int x0, int xe, int y0, int y1)
 {
     TileSpan sp;
     sp.U = sp.W = sp.TU = sp.TW = Rect{0, 0, 0, 0};
     sp.ntiles = 0;
-    if (r.x0 < r.xe && r.y0 < r.y1) {
-        sp.U = unwrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
-        sp.W = wrapped_part(vp, r.x0, r.xe, r.y0, r.y1);
+    if (x0 < xe && y0 < y1) {
+        sp.U = unwrapped_part(vp, x0, xe, y0, y1);
+        sp.W = wrapped_part(vp, x0, xe, y0, y1);
         if (!sp.U.empty()) {
             sp.TU = tiles_of_unwrapped(vp, sp.U);
             sp.ntiles += (sp.TU.xb - sp.TU.xa) * (sp.TU.yb - sp.TU.ya);
@@ -246,6 +246,10 @@ __device__ __forceinline__ TileSpan tile_span(const Viewport &vp, const TriRecor
     }
     sp.large = sp.ntiles > kSmallMaxTilesDev;
     return sp;
+}
+__device__ __forceinline__ TileSpan tile_span(const Viewport &vp, const TriRecord &r)
+{
+    return tile_span_of(vp, r.x0, r.xe, r.y0, r.y1);
 }
 
 __device__ __forceinline__ bool in_rect(const Rect &t, int tr, int tc)
