@@ -77,14 +77,9 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_setup_kernel(BatchDev 
         large = sp.large;
     }
     count_small_tiles_warp(live && !large, r, vp, sp, b.bb.tile_count + f.tile_off);
-    const unsigned m = __ballot_sync(0xffffffffu, large);
-    if (m) {
-        const int lane = threadIdx.x & 31;
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(b.bb.large_count, (uint32_t)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (large) {
-            const uint32_t q = base + __popc(m & ((1u << lane) - 1u));
+    if (__any_sync(0xffffffffu, large)) {
+        const int q = large_slot(large, sp.ntiles, b.bb.large_count, b.bb.large_cap);
+        if (q >= 0) {
             b.bb.large_queue[q] = d.local_base + t;   // frame-local draw index
             b.large_frame[q] = d.frame;
         }
@@ -128,13 +123,14 @@ __global__ void __launch_bounds__(256) batch_bin_large_kernel(BatchDev b)
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t items = *b.bb.large_count * kLargeParts;
+    const uint32_t items = large_items(b.bb.large_count);
     for (uint32_t it = warp; it < items; it += nwarps) {
-        const uint32_t q = it / kLargeParts;
+        uint32_t q, part, nparts;
+        if (!large_item(it, b.bb.large_count, b.bb.large_cap, q, part, nparts)) break;
         const BatchFrame &f = b.frames[b.large_frame[q]];
         const uint32_t gtri = b.bb.large_queue[q];
         bin_large_warp<kFill>(f.fb.records + gtri, gtri, vp_batch(f.g), b.bb.tile_count + f.tile_off,
-                              b.bb.tile_cursor + f.tile_off, b.bb.entries, b.bb.capacity, lane, it % kLargeParts);
+                              b.bb.tile_cursor + f.tile_off, b.bb.entries, b.bb.capacity, lane, part, nparts);
     }
 }
 

@@ -258,7 +258,8 @@ sloth_status build(sloth_batch *b, int shape)
     BCU(b, balloc(&b->bb.tile_offset, tiles + 1));
     BCU(b, balloc(&b->bb.tile_cursor, tiles));
     BCU(b, balloc(&b->bb.large_queue, rec));
-    BCU(b, balloc(&b->bb.large_count, 1));
+    BCU(b, balloc(&b->bb.large_count, 2));
+    b->bb.large_cap = (uint32_t)rec;
     BCU(b, balloc(&b->large_frame, rec));
     BCU(b, balloc(&b->bb.slice_offset, tiles + 4));
     BCU(b, balloc(&b->overflow, 1));
@@ -317,7 +318,7 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     if ((e = cudaMemsetAsync(b->bb.tile_count, 0, (size_t)b->total_tiles * 4, s))) return e;
     if ((e = cudaMemsetAsync(b->tile_gen, 0, (size_t)b->total_tiles * 4, s))) return e;
     if ((e = cudaMemsetAsync(b->nltree, 0xff, (size_t)b->total_nl * 4, s))) return e;
-    if ((e = cudaMemsetAsync(b->bb.large_count, 0, 4, s))) return e;
+    if ((e = cudaMemsetAsync(b->bb.large_count, 0, 8, s))) return e;
     if ((e = cudaMemsetAsync(b->fragments, 0, 8, s))) return e;
     if ((e = cudaMemsetAsync(b->overflow, 0, 4, s))) return e;
     if ((e = cudaMemcpyAsync(b->d_mats, b->h_mats, b->meshes.size() * sizeof(Mat4), cudaMemcpyHostToDevice, s)))

@@ -14,7 +14,7 @@ __device__ __forceinline__ Viewport vp_of(const FrameGeom &g)
     return Viewport{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
 }
 
-// One warp per queued large triangle.
+// Warps over the parts of the queued large triangles.
 template <bool kFill>
 __global__ void __launch_bounds__(256)
 bin_large_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
@@ -22,12 +22,14 @@ bin_large_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t items = *bb.large_count * kLargeParts;
+    const uint32_t items = large_items(bb.large_count);
     const Viewport vp = vp_of(g);
     for (uint32_t it = warp; it < items; it += nwarps) {
-        const uint32_t gtri = tri_base + bb.large_queue[it / kLargeParts];
+        uint32_t q, part, nparts;
+        if (!large_item(it, bb.large_count, bb.large_cap, q, part, nparts)) break;
+        const uint32_t gtri = tri_base + bb.large_queue[q];
         bin_large_warp<kFill>(fb.records + gtri, gtri, vp, bb.tile_count, bb.tile_cursor, bb.entries,
-                              bb.capacity, lane, it % kLargeParts);
+                              bb.capacity, lane, part, nparts);
     }
 }
 

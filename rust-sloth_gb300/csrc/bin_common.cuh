@@ -17,11 +17,59 @@ __device__ __forceinline__ uint64_t entry_key(float zlo, uint32_t gtri, bool wra
     return ((uint64_t)ordered_z(zlo) << 32) | gtri | (wrapped ? 0x80000000u : 0u);
 }
 
-// A large triangle's tiles are split among kLargeParts warps (part p takes every
-// kLargeParts-th group of 32 tiles), so that no lane walks hundreds of tiles in a row.
-constexpr uint32_t kLargeParts = 4;
+// Triangles over more than kSmallMaxTilesDev tiles are binned by warps.  Those over more
+// than kBigTiles tiles ("big") are split among kBigParts warps (part p takes every
+// kBigParts-th group of 32 tiles), so that no lane walks hundreds of tiles in a row; the
+// others take one warp each.  Big triangles are queued from the front of the queue and
+// the others from the back, and the warp items list every big part first, so that the
+// longest work starts first.
+constexpr uint32_t kBigTiles = 256;
+constexpr uint32_t kBigParts = 16;
 
-// One warp walks part `part` of a large triangle's tile rectangles: counts (kFill false)
+// Queue slot of a large triangle of this warp (called by all 32 lanes; -1 for lanes
+// without one): one atomic per class and warp.
+__device__ __forceinline__ int large_slot(bool large, uint32_t ntiles, uint32_t *large_count, uint32_t cap)
+{
+    const int lane = threadIdx.x & 31;
+    const bool big = large && ntiles > kBigTiles;
+    const unsigned mb = __ballot_sync(0xffffffffu, big), mm = __ballot_sync(0xffffffffu, large && !big);
+    uint32_t b0 = 0, m0 = 0;
+    if (lane == 0) {
+        if (mb) b0 = atomicAdd(&large_count[0], (uint32_t)__popc(mb));
+        if (mm) m0 = atomicAdd(&large_count[1], (uint32_t)__popc(mm));
+    }
+    b0 = __shfl_sync(0xffffffffu, b0, 0);
+    m0 = __shfl_sync(0xffffffffu, m0, 0);
+    const unsigned lt = (1u << lane) - 1u;
+    if (big) return (int)(b0 + __popc(mb & lt));
+    if (large) return (int)(cap - 1u - (m0 + __popc(mm & lt)));
+    return -1;
+}
+
+// Warp item i of the large queue: its queue slot, part and part count; false past the end.
+__device__ __forceinline__ bool large_item(uint32_t i, const uint32_t *large_count, uint32_t cap, uint32_t &q,
+                                           uint32_t &part, uint32_t &nparts)
+{
+    const uint32_t nb = large_count[0] * kBigParts;
+    if (i < nb) {
+        q = i / kBigParts;
+        part = i % kBigParts;
+        nparts = kBigParts;
+        return true;
+    }
+    if (i - nb >= large_count[1]) return false;
+    q = cap - 1u - (i - nb);
+    part = 0;
+    nparts = 1;
+    return true;
+}
+
+__device__ __forceinline__ uint32_t large_items(const uint32_t *large_count)
+{
+    return large_count[0] * kBigParts + large_count[1];
+}
+
+// One warp walks part `part` of `nparts` of a large triangle's tile rectangles: counts (kFill false)
 // or writes its entries (kFill true), with a per-tile depth bound (tighter than the
 // triangle-wide one).
 // The sample range (16 bytes) decides first whether the part has tiles at all; only then
@@ -29,7 +77,8 @@ constexpr uint32_t kLargeParts = 4;
 template <bool kFill>
 __device__ __forceinline__ void bin_large_warp(const TriRecord *rec, uint32_t gtri, const Viewport &vp,
                                                uint32_t *tile_count, uint32_t *tile_cursor,
-                                               uint64_t *entries, uint32_t capacity, int lane, uint32_t part)
+                                               uint64_t *entries, uint32_t capacity, int lane, uint32_t part,
+                                               uint32_t nparts)
 {
     const int4 xr = __ldg(reinterpret_cast<const int4 *>(rec) + 4);
     const TileSpan sp = tile_span_of(vp, xr.x, xr.y, xr.z, xr.w);
@@ -39,7 +88,7 @@ __device__ __forceinline__ void bin_large_warp(const TriRecord *rec, uint32_t gt
     if ((int)part * 32 >= nu + nw) return;
     const TriRecord r = *rec;
     const OrientBound ob = orient_bound(r);
-    for (int k = (int)part * 32 + lane; k < nu + nw; k += 32 * (int)kLargeParts) {
+    for (int k = (int)part * 32 + lane; k < nu + nw; k += 32 * (int)nparts) {
         int tr, tc;
         if (k < nu) {
             tr = sp.TU.ya + k / uw;

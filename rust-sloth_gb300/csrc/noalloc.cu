@@ -43,7 +43,7 @@ constexpr size_t kOffOffset = align256(kOffCount + (size_t)kMaxTiles * 4);
 constexpr size_t kOffCursor = align256(kOffOffset + ((size_t)kMaxTiles + 1) * 4);
 constexpr size_t kOffQueue = align256(kOffCursor + (size_t)kMaxTiles * 4);
 constexpr size_t kOffQCount = align256(kOffQueue + (size_t)kMaxTri * 4);
-constexpr size_t kOffGen = align256(kOffQCount + 4);
+constexpr size_t kOffGen = align256(kOffQCount + 8);
 constexpr size_t kOffNl = align256(kOffGen + (size_t)kMaxTiles * 4);
 constexpr size_t kOffFrags = align256(kOffNl + 2 * (size_t)kMaxNl * 4);
 constexpr size_t kScratchBytes = align256(kOffFrags + 8);
@@ -196,6 +196,7 @@ extern "C" sloth_status sloth_render_noalloc(const float *x, const float *y, con
     bb.tile_cursor = reinterpret_cast<uint32_t *>(base + kOffCursor);
     bb.large_queue = reinterpret_cast<uint32_t *>(base + kOffQueue);
     bb.large_count = reinterpret_cast<uint32_t *>(base + kOffQCount);
+    bb.large_cap = kMaxTri;
     bb.entries = nullptr;
     bb.capacity = 0;
     float4 *tv = reinterpret_cast<float4 *>(base + kOffTv);
@@ -206,7 +207,7 @@ extern "C" sloth_status sloth_render_noalloc(const float *x, const float *y, con
         (e = cudaMemsetAsync(fb.nltree, 0xff, 2 * (size_t)g.nl_size * sizeof(int32_t), s)) != cudaSuccess ||
         (e = cudaMemsetAsync(fb.fragments, 0, sizeof(unsigned long long), s)) != cudaSuccess ||
         (e = cudaMemsetAsync(bb.tile_count, 0, ntiles * sizeof(uint32_t), s)) != cudaSuccess ||
-        (e = cudaMemsetAsync(bb.large_count, 0, sizeof(uint32_t), s)) != cudaSuccess)
+        (e = cudaMemsetAsync(bb.large_count, 0, 2 * sizeof(uint32_t), s)) != cudaSuccess)
         return SLOTH_ERR_CUDA;
     Mat4 M;
     for (int i = 0; i < 16; ++i) M.m[i] = m[i];

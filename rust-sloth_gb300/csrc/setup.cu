@@ -5,6 +5,7 @@
 // recomputes utransform*transform per triangle and normal() per covered sample; both
 // are the same value every time, so they are formed once (matrix on the host, normal
 // here) with the same operation order (record.cuh).
+#include "bin_common.cuh"
 #include "record.cuh"
 #include "sloth_kernels.h"
 
@@ -76,13 +77,9 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, Fra
     // binning: count tiles of small triangles here, queue the rest for warps
     count_small_tiles_warp(live && !large, r, vp, sp, bb.tile_count);
     // warp-ballot compaction of the large-triangle queue
-    const unsigned m = __ballot_sync(0xffffffffu, large);
-    if (m) {
-        const int lane = threadIdx.x & 31;
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(bb.large_count, (uint32_t)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (large) bb.large_queue[base + __popc(m & ((1u << lane) - 1u))] = t;
+    if (__any_sync(0xffffffffu, large)) {
+        const int q = large_slot(large, sp.ntiles, bb.large_count, bb.large_cap);
+        if (q >= 0) bb.large_queue[q] = t;
     }
 }
 

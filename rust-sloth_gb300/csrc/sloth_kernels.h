@@ -41,8 +41,10 @@ struct BinBuffers {
     uint32_t *tile_cursor;   // ntiles
     uint64_t *entries;       // capacity: per tile, (ordered depth lower bound << 32 | draw index)
     uint32_t capacity;
-    uint32_t *large_queue;   // mesh-local triangle indices of triangles binned by warps
-    uint32_t *large_count;   // 1
+    uint32_t *large_queue;   // large_cap mesh-local indices of triangles binned by warps: big
+                             // ones from the front, the others from the back (bin_common.cuh)
+    uint32_t *large_count;   // 2: big triangles queued, other large triangles queued
+    uint32_t large_cap;
     uint32_t *slice_offset;  // ntiles + 4: per tile the first raster item of its slices;
                              // [ntiles] = items, [ntiles+1] = split threshold, [ntiles+2] =
                              // slice size, [ntiles+3] = items of split tiles (listed first)
