@@ -72,6 +72,7 @@ struct sloth_ctx {
     float4 *tv = nullptr;
     size_t tv_cap = 0;
     uint32_t *h_total = nullptr;   // pinned
+    cudaEvent_t total_ev = nullptr;   // h_total has arrived
     unsigned long long *h_frags = nullptr;   // pinned
     uint32_t *h_error = nullptr;   // pinned copy of fb.error
     uint32_t tri_base = 0;
@@ -391,11 +392,13 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
         ctx->own_stream = true;
     }
     if (cudaMallocHost(&ctx->h_total, sizeof(uint32_t)) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->total_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost(&ctx->h_frags, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMallocHost(&ctx->h_error, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->fb.error, sizeof(uint32_t)) != cudaSuccess ||
         cudaMemset(ctx->fb.error, 0, sizeof(uint32_t)) != cudaSuccess) {
         if (ctx->h_total) cudaFreeHost(ctx->h_total);
+        if (ctx->total_ev) cudaEventDestroy(ctx->total_ev);
         if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
         if (ctx->h_error) cudaFreeHost(ctx->h_error);
         if (ctx->fb.error) cudaFree(ctx->fb.error);
@@ -430,6 +433,7 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     dfree(ctx->bb.items);
     dfree(ctx->tv);
     if (ctx->h_total) cudaFreeHost(ctx->h_total);
+    if (ctx->total_ev) cudaEventDestroy(ctx->total_ev);
     if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
     if (ctx->h_error) cudaFreeHost(ctx->h_error);
     dfree(ctx->fb.error);
@@ -760,16 +764,30 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
     CU(ctx, cudaMemcpyAsync(ctx->h_total, ctx->bb.tile_offset + ntiles, sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, s));
-    CU(ctx, cudaStreamSynchronize(s));
+    CU(ctx, cudaEventRecord(ctx->total_ev, s));
+    // The entry count sizes the entry buffer.  With a buffer from earlier draws the fill
+    // kernels go ahead with it while the host waits for the count (they write no slot past
+    // the capacity); only a count above the capacity makes the host grow the buffer and
+    // fill again, after a scan that resets the cursors.
+    auto fill = [&]() -> sloth_status {
+        CU(ctx, timed(ctx, "bin_fill", [&] { return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+        CU(ctx, timed(ctx, "bin_fill_large", [&] { return launch_bin_fill_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+        return SLOTH_OK;
+    };
+    const bool ahead = ctx->bb.entries && ctx->bb.capacity > 0;
+    if (ahead && (st = fill()) != SLOTH_OK) return st;
+    CU(ctx, cudaEventSynchronize(ctx->total_ev));
     const uint32_t total = *ctx->h_total;
-    size_t ecap = ctx->bb.capacity;
-    if ((st = ensure_scratch(ctx, &ctx->bb.entries, &ecap, total)) != SLOTH_OK) return st;
-    ctx->bb.capacity = (uint32_t)(ecap > 0xffffffffu ? 0xffffffffu : ecap);
+    if (!ahead || total > ctx->bb.capacity) {
+        size_t ecap = ctx->bb.capacity;
+        if ((st = ensure_scratch(ctx, &ctx->bb.entries, &ecap, total)) != SLOTH_OK) return st;
+        ctx->bb.capacity = (uint32_t)(ecap > 0xffffffffu ? 0xffffffffu : ecap);
+        if (ahead) CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
+        if ((st = fill()) != SLOTH_OK) return st;
+    }
     size_t icap = ctx->bb.item_capacity;
     if ((st = ensure_scratch(ctx, &ctx->bb.items, &icap, raster_item_bound(ntiles, total))) != SLOTH_OK) return st;
     ctx->bb.item_capacity = (uint32_t)icap;
-    CU(ctx, timed(ctx, "bin_fill", [&] { return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
-    CU(ctx, timed(ctx, "bin_fill_large", [&] { return launch_bin_fill_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_items", [&] { return launch_bin_items(ntiles, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "raster", [&] { return launch_raster(g, ctx->fb, ctx->bb, ctx->depth_cull, s); }));
     ctx->tri_base += mesh->ntri;

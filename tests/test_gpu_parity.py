@@ -226,6 +226,21 @@ def test_clear_redraw_and_resize(ctx):
         assert_same(gpu_render(ctx, [m], R, w, h, im, dev_meshes=[dm]), ref, f"{w}x{h}")
 
 
+def test_entry_buffer_grows_between_frames():
+    """A frame with many more tile entries than the context's earlier frames: the fill that
+    went ahead with the old entry buffer is redone after the buffer grows."""
+    c = S.Context(0)
+    try:
+        small = W.soup(200, seed=4)
+        big = W.soup(20000, seed=5, n_large=60)
+        R = O.euler_rotation(*W.cli_rotation())
+        for m, (w, h) in [(small, (200, 100)), (big, (480, 270)), (small, (200, 100)), (big, (960, 540))]:
+            ref = oracle_render([m], R, w, h, True)
+            assert_same(gpu_render(c, [m], R, w, h, True), ref, f"{m['rgb'].shape[0]} triangles {w}x{h}")
+    finally:
+        c.close()
+
+
 def test_many_frames_generation_counter(ctx):
     """Repeated clears reuse the key buffer through the tile generation counter."""
     m = W.soup(300, seed=1)
