@@ -338,43 +338,80 @@ def run_gpu(args):
         for _ in range(args.steps):
             serial_step()
         serial_s = time.perf_counter() - t0
-        # pipelined: two contexts in turn, each with its own mesh buffers and host outputs;
-        # a frame's read-back overlaps the next frame's upload and draw
-        ctx2 = S.Context(local)
-        ctx2.set_viewport(W_PX, H_PX, True)
-        dm2 = S.Mesh(ctx2, m["x"], m["y"], m["z"], m["rgb"])
-        ctx2.update([dm2])
-        ctx2.set_depth_cull(not args.no_depth_cull)
-        lanes = [(ctx, dm, *host_out()), (ctx2, dm2, *host_out())]
+        # pipelined: contexts in turn, each with its own stream, mesh buffers and host
+        # outputs; a frame's upload, draw and read-back overlap the other contexts' frames
+        extra = []
+        for _ in range(args.e2e_contexts - 1):
+            c2 = S.Context(local)
+            c2.set_viewport(W_PX, H_PX, True)
+            d2 = S.Mesh(c2, m["x"], m["y"], m["z"], m["rgb"])
+            c2.update([d2])
+            c2.set_depth_cull(not args.no_depth_cull)
+            extra.append((c2, d2))
+        lanes = [(ctx, dm, *host_out())] + [(c2, d2, *host_out()) for c2, d2 in extra]
+        nl = len(lanes)
 
-        def pipelined_step(i):
-            c, mm, oc, oz = lanes[i & 1]
+        def frame_on(lane):
+            c, mm, oc, oz = lane
             c.synchronize()            # this context's previous frame (and its read-back) is done
             mm.update(hx, hy, hz, hrgb)
             c.clear()
             c.draw_mesh(mm, R)
             c.read_into_async(oc, oz)
 
-        for i in range(max(2, args.warmup)):
-            pipelined_step(i)
-        ctx.synchronize()
-        ctx2.synchronize()
+        def sync_all():
+            for lane in lanes:
+                lane[0].synchronize()
+
+        # one host thread: the contexts in turn
+        for i in range(max(nl, args.warmup)):
+            frame_on(lanes[i % nl])
+        sync_all()
         if ws > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
         for i in range(args.steps):
-            pipelined_step(i)
-        ctx.synchronize()
-        ctx2.synchronize()
+            frame_on(lanes[i % nl])
+        sync_all()
+        one_thread_s = time.perf_counter() - t0
+        # one host thread per context (the library calls release the interpreter lock), so
+        # that a thread waiting inside a draw for its entry count holds back no other context
+        import threading
+        start = threading.Barrier(nl + 1)
+        errors = []
+
+        def worker(k):
+            try:
+                start.wait()
+                for i in range(k, args.steps, nl):
+                    frame_on(lanes[k])
+                lanes[k][0].synchronize()
+            except Exception as exc:   # reported after the join
+                errors.append(exc)
+
+        threads = [threading.Thread(target=worker, args=(k,)) for k in range(nl)]
+        for th in threads:
+            th.start()
+        if ws > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        start.wait()
+        for th in threads:
+            th.join()
         e2e_s = time.perf_counter() - t0
+        if errors:
+            raise errors[0]
         # the pipelined frames equal the serial ones
-        assert np.array_equal(lanes[0][2], hc) and np.array_equal(lanes[1][2], hc)
-        e2e_s, serial_s = max_over_ranks([e2e_s, serial_s], dev, ws)
+        assert all(np.array_equal(lane[2], hc) for lane in lanes)
+        e2e_s, serial_s, one_thread_s = max_over_ranks([e2e_s, serial_s, one_thread_s], dev, ws)
         e2e = {"value": whole_job_rate(args.steps, ws, e2e_s), "unit": "frames/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h,
-               "pipeline": "two contexts in turn: a frame's read-back overlaps the next frame's upload and draw",
+               "pipeline": f"{nl} contexts, one stream and one host thread each: a frame's upload, draw and "
+                           "read-back overlap the other contexts' frames",
+               "one_thread_value": whole_job_rate(args.steps, ws, one_thread_s),
                "serial_value": whole_job_rate(args.steps, ws, serial_s)}
-        ctx2.close()
+        for c2, _ in extra:
+            c2.close()
 
     if rank != 0:
         if ws > 1:
@@ -726,6 +763,7 @@ def main():
     ap.add_argument("--no-depth-cull", action="store_true",
                     help="rasterize every triangle (SLOTH_OPTION_DEPTH_CULL 0)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
+    ap.add_argument("--e2e-contexts", type=int, default=4, help="contexts (one host thread each) in the end-to-end leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched config-3 leg")
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable legs (configs 4 and 5)")

@@ -11,6 +11,7 @@ raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb, uint32_t ntiles, int 
 {
     __shared__ TileSmem<TW, TH> S;
     if (blockIdx.x >= bb.slice_offset[ntiles] || blockIdx.x >= bb.item_capacity) return;
+    if (bb.tile_offset[ntiles] > bb.capacity) return;   // entries past the buffer: the host runs it again
     const uint2 it = bb.items[blockIdx.x];
     const uint32_t all = bb.tile_count[it.x];
     const uint32_t thr = bb.slice_offset[ntiles + 1], slice = bb.slice_offset[ntiles + 2];

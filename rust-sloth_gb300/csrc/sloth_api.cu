@@ -765,17 +765,25 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     CU(ctx, cudaMemcpyAsync(ctx->h_total, ctx->bb.tile_offset + ntiles, sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, s));
     CU(ctx, cudaEventRecord(ctx->total_ev, s));
-    // The entry count sizes the entry buffer.  With a buffer from earlier draws the fill
-    // kernels go ahead with it while the host waits for the count (they write no slot past
-    // the capacity); only a count above the capacity makes the host grow the buffer and
-    // fill again, after a scan that resets the cursors.
-    auto fill = [&]() -> sloth_status {
+    // The entry count sizes the entry buffer.  With a buffer from earlier draws the rest of
+    // the draw goes ahead with it while the host waits for the count: the fill kernels
+    // write no slot past the capacity and the raster does nothing when the count is above
+    // it.  Only then does the host grow the buffer and run the rest again, after a scan
+    // that resets the cursors.
+    auto rest = [&](size_t entries_bound) -> sloth_status {
         CU(ctx, timed(ctx, "bin_fill", [&] { return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
         CU(ctx, timed(ctx, "bin_fill_large", [&] { return launch_bin_fill_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+        size_t icap = ctx->bb.item_capacity;
+        sloth_status st2;
+        if ((st2 = ensure_scratch(ctx, &ctx->bb.items, &icap, raster_item_bound(ntiles, entries_bound))) != SLOTH_OK)
+            return st2;
+        ctx->bb.item_capacity = (uint32_t)icap;
+        CU(ctx, timed(ctx, "bin_items", [&] { return launch_bin_items(ntiles, g, ctx->fb, ctx->bb, s); }));
+        CU(ctx, timed(ctx, "raster", [&] { return launch_raster(g, ctx->fb, ctx->bb, ctx->depth_cull, s); }));
         return SLOTH_OK;
     };
     const bool ahead = ctx->bb.entries && ctx->bb.capacity > 0;
-    if (ahead && (st = fill()) != SLOTH_OK) return st;
+    if (ahead && (st = rest(ctx->bb.capacity)) != SLOTH_OK) return st;
     CU(ctx, cudaEventSynchronize(ctx->total_ev));
     const uint32_t total = *ctx->h_total;
     if (!ahead || total > ctx->bb.capacity) {
@@ -783,13 +791,8 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
         if ((st = ensure_scratch(ctx, &ctx->bb.entries, &ecap, total)) != SLOTH_OK) return st;
         ctx->bb.capacity = (uint32_t)(ecap > 0xffffffffu ? 0xffffffffu : ecap);
         if (ahead) CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
-        if ((st = fill()) != SLOTH_OK) return st;
+        if ((st = rest(total)) != SLOTH_OK) return st;
     }
-    size_t icap = ctx->bb.item_capacity;
-    if ((st = ensure_scratch(ctx, &ctx->bb.items, &icap, raster_item_bound(ntiles, total))) != SLOTH_OK) return st;
-    ctx->bb.item_capacity = (uint32_t)icap;
-    CU(ctx, timed(ctx, "bin_items", [&] { return launch_bin_items(ntiles, g, ctx->fb, ctx->bb, s); }));
-    CU(ctx, timed(ctx, "raster", [&] { return launch_raster(g, ctx->fb, ctx->bb, ctx->depth_cull, s); }));
     ctx->tri_base += mesh->ntri;
     ctx->dirty = true;
     return SLOTH_OK;
