@@ -14,7 +14,6 @@
 //
 // Scratch layout (byte offsets into g_noalloc_scratch):
 //   records   kMaxTri x 96 B          per-triangle setup records
-//   tv        3*kMaxTri x 16 B        transformed vertices
 //   keys      kMaxCells x 8 B         depth keys (tiles padded to 64x32 cells)
 //   bins      tile counts/offsets/cursors, the large-triangle queue and its counter
 //   tile_gen  kMaxTiles x 4 B         tile generations (cleared every call)
@@ -36,8 +35,7 @@ constexpr uint32_t kMaxTiles = kMaxCells / (kTileW * kTileH);
 
 constexpr size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 constexpr size_t kOffRecords = 0;
-constexpr size_t kOffTv = align256(kOffRecords + (size_t)kMaxTri * sizeof(TriRecord));
-constexpr size_t kOffKeys = align256(kOffTv + 3 * (size_t)kMaxTri * sizeof(float4));
+constexpr size_t kOffKeys = align256(kOffRecords + (size_t)kMaxTri * sizeof(TriRecord));
 constexpr size_t kOffCount = align256(kOffKeys + (size_t)kMaxCells * sizeof(uint64_t));
 constexpr size_t kOffOffset = align256(kOffCount + (size_t)kMaxTiles * 4);
 constexpr size_t kOffCursor = align256(kOffOffset + ((size_t)kMaxTiles + 1) * 4);
@@ -199,7 +197,6 @@ extern "C" sloth_status sloth_render_noalloc(const float *x, const float *y, con
     bb.large_cap = kMaxTri;
     bb.entries = nullptr;
     bb.capacity = 0;
-    float4 *tv = reinterpret_cast<float4 *>(base + kOffTv);
 
     // The array keeps the previous call's contents: reset what must start empty.
     cudaError_t e;
@@ -212,8 +209,7 @@ extern "C" sloth_status sloth_render_noalloc(const float *x, const float *y, con
     Mat4 M;
     for (int i = 0; i < 16; ++i) M.m[i] = m[i];
     MeshDev md{x, y, z, nullptr, rgb, 3 * ntri, ntri};
-    if (launch_vertex_transform(md, M, tv, s) != cudaSuccess) return SLOTH_ERR_CUDA;
-    if (launch_setup(md, tv, 0, g, fb, bb, s) != cudaSuccess) return SLOTH_ERR_CUDA;
+    if (launch_setup(md, nullptr, M, 0, g, fb, bb, s) != cudaSuccess) return SLOTH_ERR_CUDA;
     if (launch_newline(ntri, 0, g, fb, s) != cudaSuccess) return SLOTH_ERR_CUDA;
     if (ntri) {
         noalloc_raster_kernel<<<ntiles, 256, 0, s>>>(ntri, g, fb);

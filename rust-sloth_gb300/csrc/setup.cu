@@ -50,8 +50,17 @@ __device__ __forceinline__ Viewport to_vp(const FrameGeom &g)
     return Viewport{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
 }
 
+// One vertex of a soup transformed in place: (M*v).xyz with the vertex kernel's operations.
+__device__ __forceinline__ float4 transform_vertex(const MeshDev &mesh, const Mat4 &M, uint32_t i)
+{
+    const float x = __ldg(mesh.x + i), y = __ldg(mesh.y + i), z = __ldg(mesh.z + i);
+    return make_float4(row_dot(&M.m[0], x, y, z), row_dot(&M.m[4], x, y, z), row_dot(&M.m[8], x, y, z), 0.0f);
+}
+
+// tv null (soups): each thread transforms its triangle's three vertices itself, which
+// saves the vertex kernel and its round trip through memory.
 __global__ void __launch_bounds__(256)
-setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, FrameGeom g,
+setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_base, FrameGeom g,
              FrameBuffers fb, BinBuffers bb)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -69,7 +78,11 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, uint32_t tri_base, Fra
         } else {
             i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
         }
-        r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), mesh.rgb + 3 * (size_t)t, g.w, g.h);
+        if (tv)
+            r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), mesh.rgb + 3 * (size_t)t, g.w, g.h);
+        else
+            r = build_record(transform_vertex(mesh, M, i1), transform_vertex(mesh, M, i2),
+                             transform_vertex(mesh, M, i3), mesh.rgb + 3 * (size_t)t, g.w, g.h);
         fb.records[tri_base + t] = r;
         sp = tile_span(vp, r);
         large = sp.large;
@@ -142,12 +155,12 @@ cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *
     return cudaGetLastError();
 }
 
-cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, uint32_t tri_base,
+cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, uint32_t tri_base,
                          const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
                          cudaStream_t s)
 {
     if (mesh.ntri == 0) return cudaSuccess;
-    setup_kernel<<<(mesh.ntri + 255) / 256, 256, 0, s>>>(mesh, tv, tri_base, g, fb, bb);
+    setup_kernel<<<(mesh.ntri + 255) / 256, 256, 0, s>>>(mesh, tv, M, tri_base, g, fb, bb);
     return cudaGetLastError();
 }
 

@@ -744,7 +744,7 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     CU(ctx, cudaSetDevice(ctx->device));
     sloth_status st;
     if ((st = ensure_records(ctx, (size_t)ctx->tri_base + mesh->ntri)) != SLOTH_OK) return st;
-    if ((st = ensure_scratch(ctx, &ctx->tv, &ctx->tv_cap, mesh->nvert)) != SLOTH_OK) return st;
+    if (mesh->idx && (st = ensure_scratch(ctx, &ctx->tv, &ctx->tv_cap, mesh->nvert)) != SLOTH_OK) return st;
     if ((st = ensure_scratch(ctx, &ctx->bb.large_queue, &ctx->large_cap, mesh->ntri)) != SLOTH_OK) return st;
     if (!ctx->bb.large_count) CU(ctx, dalloc(&ctx->bb.large_count, 2));
     ctx->bb.large_cap = mesh->ntri;
@@ -757,8 +757,10 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     cudaStream_t s = ctx->stream;
     CU(ctx, cudaMemsetAsync(ctx->bb.tile_count, 0, ntiles * sizeof(uint32_t), s));
     CU(ctx, cudaMemsetAsync(ctx->bb.large_count, 0, 2 * sizeof(uint32_t), s));
-    CU(ctx, timed(ctx, "vertex", [&] { return launch_vertex_transform(md, M, ctx->tv, s); }));
-    CU(ctx, timed(ctx, "setup", [&] { return launch_setup(md, ctx->tv, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+    // indexed meshes share vertices: transformed once by the vertex kernel; soups in setup
+    const float4 *tv = mesh->idx ? ctx->tv : nullptr;
+    if (tv) CU(ctx, timed(ctx, "vertex", [&] { return launch_vertex_transform(md, M, ctx->tv, s); }));
+    CU(ctx, timed(ctx, "setup", [&] { return launch_setup(md, tv, M, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "newline", [&] { return launch_newline(mesh->ntri, ctx->tri_base, g, ctx->fb, s); }));
     CU(ctx, timed(ctx, "bin_count_large",[&] { return launch_bin_count_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));

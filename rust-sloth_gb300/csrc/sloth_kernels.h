@@ -95,8 +95,9 @@ cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *
                                     cudaStream_t s);
 
 // per-triangle setup: records[tri_base + t], small-triangle tile counts and newline rows,
-// large-triangle queue.
-cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, uint32_t tri_base,
+// large-triangle queue.  tv: the vertex kernel's output, or null to transform by M here
+// (soups only: mesh.idx null).
+cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, uint32_t tri_base,
                          const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
                          cudaStream_t s);
 // newline sentinels (image mode): fold each triangle's row range into the segment tree.
