@@ -4,16 +4,18 @@
 
 namespace sloth {
 
-// Pairs of frame cells; each warp takes 32 consecutive pairs (resolve_pair).
-__global__ void __launch_bounds__(256) resolve_kernel(FrameGeom g, FrameBuffers fb)
+// Runs of kRun frame cells; each warp takes 32 consecutive runs (resolve_run).
+constexpr int kRun = 2;
+
+__global__ void __launch_bounds__(256) resolve_kernel(FrameGeom g, FrameBuffers fb, int vec)
 {
     const uint64_t nz = (uint64_t)g.w * g.h;
     const uint64_t ncells = g.image ? nz + g.h : nz;
-    const uint64_t npairs = (ncells + 1) / 2;
+    const uint64_t nruns = (ncells + kRun - 1) / kRun;
     const int lane = threadIdx.x & 31;
-    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < npairs; base += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < nruns; base += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t p = base + threadIdx.x;
-        resolve_pair(g, fb, p, p < npairs, lane);
+        resolve_run<kRun>(g, fb, p, p < nruns, lane, vec != 0);
     }
 }
 
@@ -21,9 +23,11 @@ cudaError_t launch_resolve(const FrameGeom &g, const FrameBuffers &fb, cudaStrea
 {
     const uint64_t ncells = (uint64_t)g.w * g.h + (g.image ? g.h : 0);
     if (ncells == 0) return cudaSuccess;
-    uint64_t blocks = ((ncells + 1) / 2 + 255) / 256;
+    uint64_t blocks = ((ncells + kRun - 1) / kRun + 255) / 256;
     if (blocks > 152u * 32u) blocks = 152u * 32u;
-    resolve_kernel<<<(unsigned)blocks, 256, 0, s>>>(g, fb);
+    const int vec = ((reinterpret_cast<uintptr_t>(fb.cells_out) | reinterpret_cast<uintptr_t>(fb.z_out) |
+                      reinterpret_cast<uintptr_t>(fb.winner_out)) & (4u * kRun - 1u)) == 0;
+    resolve_kernel<<<(unsigned)blocks, 256, 0, s>>>(g, fb, vec);
     return cudaGetLastError();
 }
 

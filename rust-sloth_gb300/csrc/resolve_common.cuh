@@ -33,10 +33,12 @@ __device__ __forceinline__ bool later(const Cand &a, const Cand &b)
 
 __device__ __forceinline__ uint64_t key_at(const FrameGeom &g, const FrameBuffers &fb, int r, int cc)
 {
-    // tile sides are powers of two
+    // tile sides are powers of two; both reads issued before either is tested (the key
+    // of a tile of an older generation is in bounds, only stale)
     const int tile = (r >> (__ffs(g.th) - 1)) * g.ntx + (cc >> (__ffs(g.tw) - 1));
-    if (fb.tile_gen[tile] != fb.gen) return kEmptyKey;
-    return fb.keys[(size_t)r * g.pitch + cc];
+    const uint32_t gen = __ldg(fb.tile_gen + tile);
+    const uint64_t k = __ldg(reinterpret_cast<const unsigned long long *>(fb.keys) + (size_t)r * g.pitch + cc);
+    return gen == fb.gen ? k : kEmptyKey;
 }
 
 // Rebuild the winning write of depth cell (r, cc) from its key.
@@ -53,11 +55,13 @@ __device__ __forceinline__ Cand decode(const FrameGeom &g, const FrameBuffers &f
         c.y = r - 1;
         c.x = (cc + g.w) >> 1;
     }
+    // rows 0-3 (vertices, edges, depth) and 5 (shade, colour); row 4 is not needed
     const float4 *p = reinterpret_cast<const float4 *>(fb.records + c.tri);
     TriRecord rec;
     float4 *o = reinterpret_cast<float4 *>(&rec);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) o[k] = __ldg(p + k);
+    for (int k = 0; k < 4; ++k) o[k] = __ldg(p + k);
+    o[5] = __ldg(p + 5);
     const EdgeVals e = eval_edges(rec, (float)c.x, (float)c.y);
     const float shade = fmul(rec.na, fadd(fadd(e.w0, e.w1), e.w2));
     if (z_out) *z_out = interp_z(rec.v1z, rec.dz2, rec.dz3, rec.a, e.w1, e.w2);
@@ -231,6 +235,116 @@ __device__ __forceinline__ void resolve_pair(const FrameGeom &g, const FrameBuff
     if (c0 + 1 < nz) {
         fb.z_out[c0 + 1] = z1;
         fb.winner_out[c0 + 1] = h1 ? (int32_t)k1.tri : -1;
+    }
+}
+
+// Resolve frame cells c0 = K*p .. c0+K-1 and the depth cells among them, of one frame
+// (the rule of resolve_cell).  Called by all 32 lanes of a warp with consecutive p in
+// lane order; lanes with valid false (past the end) write nothing.  Depth cell c0-1's
+// winner is the previous lane's last depth cell (lane 0 decodes it itself).  With vec the
+// outputs are 4K-byte aligned and a lane's K cells go out in one store per buffer.
+template <int K>
+__device__ __forceinline__ void resolve_run(const FrameGeom &g, const FrameBuffers &fb, uint64_t p, bool valid,
+                                            int lane, bool vec)
+{
+    static_assert(K == 2 || K == 4, "one 8- or 16-byte store per lane and buffer");
+    const uint64_t nz = (uint64_t)g.w * g.h;
+    const uint64_t ncells = g.image ? nz + g.h : nz;
+    const uint64_t c0 = K * p;
+    int r0 = 0, cc0 = 0;
+    if (valid && c0 < nz) {
+        if (nz <= 0xffffffffull) {
+            r0 = (int)((uint32_t)c0 / (uint32_t)g.w);
+        } else {
+            r0 = (int)(c0 / (uint64_t)g.w);
+        }
+        cc0 = (int)(c0 - (uint64_t)r0 * g.w);
+    }
+    int rj[K], cj[K];
+    uint64_t key[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        rj[j] = j == 0 ? r0 : (cj[j - 1] + 1 == g.w ? rj[j - 1] + 1 : rj[j - 1]);
+        cj[j] = j == 0 ? cc0 : (cj[j - 1] + 1 == g.w ? 0 : cj[j - 1] + 1);
+        key[j] = valid && c0 + j < nz ? key_at(g, fb, rj[j], cj[j]) : kEmptyKey;
+    }
+    Cand kc[K];
+    bool hc[K];
+    float z[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        kc[j] = Cand{0, 0, 0, (uint32_t)' '};
+        hc[j] = key[j] != kEmptyKey;
+        z[j] = kFltMax;
+        if (hc[j]) kc[j] = decode(g, fb, key[j], rj[j], cj[j], &z[j]);
+    }
+    // depth cell c0-1
+    Cand km = shfl_up_cand(kc[K - 1]);
+    bool hm = __shfl_up_sync(0xffffffffu, (int)hc[K - 1], 1) != 0;
+    if (lane == 0) {
+        hm = false;
+        if (valid && c0 >= 1 && c0 - 1 < nz) {
+            int rm, cm;
+            if (c0 < nz) {
+                rm = cc0 > 0 ? r0 : r0 - 1;
+                cm = cc0 > 0 ? cc0 - 1 : g.w - 1;
+            } else {
+                rm = g.h - 1;
+                cm = g.w - 1;
+            }
+            const uint64_t k = key_at(g, fb, rm, cm);
+            if (k != kEmptyKey) {
+                km = decode(g, fb, k, rm, cm, nullptr);
+                hm = true;
+            }
+        }
+    }
+    if (!valid) return;
+    // frame cell c: depth cells c and c-1, newline
+    uint32_t out[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        const uint64_t c = c0 + j;
+        bool have = hc[j];
+        Cand best = kc[j];
+        const Cand &prev = j == 0 ? km : kc[j - 1];
+        const bool hprev = j == 0 ? hm : hc[j - 1];
+        if (hprev && (!have || later(prev, best))) {
+            best = prev;
+            have = true;
+        }
+        Cand n;
+        if (c < ncells && newline_at(g, fb, c, nz, rj[j], cj[j], n) && (!have || later(n, best))) best = n;
+        out[j] = best.cell;
+    }
+    if (vec && c0 + K <= ncells) {
+        if constexpr (K == 4)
+            *reinterpret_cast<uint4 *>(fb.cells_out + c0) = make_uint4(out[0], out[1], out[2], out[3]);
+        else
+            *reinterpret_cast<uint2 *>(fb.cells_out + c0) = make_uint2(out[0], out[1]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; ++j)
+            if (c0 + j < ncells) fb.cells_out[c0 + j] = out[j];
+    }
+    if (vec && c0 + K <= nz) {
+        int32_t wv[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) wv[j] = hc[j] ? (int32_t)kc[j].tri : -1;
+        if constexpr (K == 4) {
+            *reinterpret_cast<float4 *>(fb.z_out + c0) = make_float4(z[0], z[1], z[2], z[3]);
+            *reinterpret_cast<int4 *>(fb.winner_out + c0) = make_int4(wv[0], wv[1], wv[2], wv[3]);
+        } else {
+            *reinterpret_cast<float2 *>(fb.z_out + c0) = make_float2(z[0], z[1]);
+            *reinterpret_cast<int2 *>(fb.winner_out + c0) = make_int2(wv[0], wv[1]);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; ++j)
+            if (c0 + j < nz) {
+                fb.z_out[c0 + j] = z[j];
+                fb.winner_out[c0 + j] = hc[j] ? (int32_t)kc[j].tri : -1;
+            }
     }
 }
 
