@@ -147,6 +147,31 @@ cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
     return cudaGetLastError();
 }
 
+// The resets of a frame (device error word, fragment counter, newline tree: frame) and of
+// a draw (tile entry counts, large-queue counters: draw) in one launch.
+__global__ void __launch_bounds__(256)
+frame_reset_kernel(FrameBuffers fb, BinBuffers bb, uint32_t nl_nodes, uint32_t ntiles, int frame, int draw)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (frame && i < nl_nodes) fb.nltree[i] = -1;
+    if (draw && i < ntiles) bb.tile_count[i] = 0u;
+    if (i == 0) {
+        if (frame) {
+            *fb.error = 0u;
+            *fb.fragments = 0ull;
+        }
+        if (draw) bb.large_count[0] = bb.large_count[1] = 0u;
+    }
+}
+
+cudaError_t launch_frame_reset(const FrameBuffers &fb, const BinBuffers &bb, uint32_t nl_nodes, uint32_t ntiles,
+                               bool frame, bool draw, cudaStream_t s)
+{
+    const uint32_t n = max(frame ? nl_nodes : 1u, draw ? ntiles : 1u);
+    frame_reset_kernel<<<(n + 255) / 256, 256, 0, s>>>(fb, bb, nl_nodes, ntiles, frame ? 1 : 0, draw ? 1 : 0);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *tv, cudaStream_t s)
 {
     if (mesh.nvert == 0) return cudaSuccess;

@@ -77,6 +77,9 @@ struct sloth_ctx {
     uint32_t *h_error = nullptr;   // pinned copy of fb.error
     uint32_t tri_base = 0;
     bool dirty = true;
+    bool reset_pending = false;    // a clear's resets, folded into the next launch that needs them
+    cudaStream_t side = nullptr;   // the entry-count copy, off the draw's stream
+    cudaEvent_t scan_ev = nullptr;
 
     // instrumentation
     int depth_cull = 1;
@@ -241,9 +244,24 @@ static sloth_status ensure_scratch(sloth_ctx *ctx, T **p, size_t *cap, size_t ne
     return SLOTH_OK;
 }
 
+// A clear's resets (error word, fragments, newline tree) wait for the next launch that
+// reads them; a draw adds its own (tile counts, large-queue counters) to the same launch.
+static sloth_status apply_resets(sloth_ctx *ctx, bool draw)
+{
+    if (!ctx->reset_pending && !draw) return SLOTH_OK;
+    CU(ctx, launch_frame_reset(ctx->fb, ctx->bb, 2u * (uint32_t)ctx->g.nl_size, (uint32_t)(ctx->g.ntx * ctx->g.nty),
+                               ctx->reset_pending, draw, ctx->stream));
+    ctx->reset_pending = false;
+    return SLOTH_OK;
+}
+
 // The device error word travels with the next synchronising call's copies.
 static sloth_status queue_error_copy(sloth_ctx *ctx)
 {
+    if (ctx->have_frame) {
+        sloth_status st0 = apply_resets(ctx, false);
+        if (st0 != SLOTH_OK) return st0;
+    }
     CU(ctx, cudaMemcpyAsync(ctx->h_error, ctx->fb.error, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     return SLOTH_OK;
 }
@@ -261,6 +279,8 @@ static sloth_status resolve_pending(sloth_ctx *ctx)
 {
     if (!ctx->have_frame)
         return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "the context has no frame: call sloth_ctx_clear first");
+    sloth_status st0 = apply_resets(ctx, false);
+    if (st0 != SLOTH_OK) return st0;
     if (!ctx->dirty) return SLOTH_OK;
     CU(ctx, timed(ctx, "resolve", [&] { return launch_resolve(ctx->g, ctx->fb, ctx->stream); }));
     ctx->dirty = false;
@@ -393,12 +413,16 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
     }
     if (cudaMallocHost(&ctx->h_total, sizeof(uint32_t)) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->total_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->scan_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMallocHost(&ctx->h_frags, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMallocHost(&ctx->h_error, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->fb.error, sizeof(uint32_t)) != cudaSuccess ||
         cudaMemset(ctx->fb.error, 0, sizeof(uint32_t)) != cudaSuccess) {
         if (ctx->h_total) cudaFreeHost(ctx->h_total);
         if (ctx->total_ev) cudaEventDestroy(ctx->total_ev);
+        if (ctx->scan_ev) cudaEventDestroy(ctx->scan_ev);
+        if (ctx->side) cudaStreamDestroy(ctx->side);
         if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
         if (ctx->h_error) cudaFreeHost(ctx->h_error);
         if (ctx->fb.error) cudaFree(ctx->fb.error);
@@ -434,6 +458,8 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     dfree(ctx->tv);
     if (ctx->h_total) cudaFreeHost(ctx->h_total);
     if (ctx->total_ev) cudaEventDestroy(ctx->total_ev);
+    if (ctx->scan_ev) cudaEventDestroy(ctx->scan_ev);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
     if (ctx->h_error) cudaFreeHost(ctx->h_error);
     dfree(ctx->fb.error);
@@ -487,16 +513,15 @@ sloth_status sloth_ctx_clear(sloth_ctx *ctx)
         sloth_status st = alloc_frame(ctx);
         if (st != SLOTH_OK) return st;
     }
-    // A new frame starts without a device error.
-    CU(ctx, cudaMemsetAsync(ctx->fb.error, 0, sizeof(uint32_t), ctx->stream));
+    // A new frame starts without a device error, fragments or newlines (reset by the next
+    // launch that needs them).
+    ctx->reset_pending = true;
     // A new generation invalidates every tile's keys without touching them.
     ctx->fb.gen++;
     if (ctx->fb.gen == 0) {
         CU(ctx, cudaMemsetAsync(ctx->fb.tile_gen, 0, ctx->ntiles_cap * sizeof(uint32_t), ctx->stream));
         ctx->fb.gen = 1;
     }
-    CU(ctx, cudaMemsetAsync(ctx->fb.nltree, 0xff, 2 * (size_t)ctx->g.nl_size * sizeof(int32_t), ctx->stream));
-    CU(ctx, cudaMemsetAsync(ctx->fb.fragments, 0, sizeof(unsigned long long), ctx->stream));
     ctx->tri_base = 0;
     ctx->dirty = true;
     return SLOTH_OK;
@@ -617,9 +642,11 @@ sloth_status sloth_ctx_fragments(sloth_ctx *ctx, uint64_t *fragments)
         return SLOTH_OK;
     }
     CU(ctx, cudaSetDevice(ctx->device));
+    sloth_status st = apply_resets(ctx, false);
+    if (st != SLOTH_OK) return st;
     CU(ctx, cudaMemcpyAsync(ctx->h_frags, ctx->fb.fragments, sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, ctx->stream));
-    sloth_status st = queue_error_copy(ctx);
+    st = queue_error_copy(ctx);
     if (st != SLOTH_OK) return st;
     CU(ctx, cudaStreamSynchronize(ctx->stream));
     *fragments = *ctx->h_frags;
@@ -755,8 +782,7 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     const FrameGeom &g = ctx->g;
     const uint32_t ntiles = (uint32_t)(g.ntx * g.nty);
     cudaStream_t s = ctx->stream;
-    CU(ctx, cudaMemsetAsync(ctx->bb.tile_count, 0, ntiles * sizeof(uint32_t), s));
-    CU(ctx, cudaMemsetAsync(ctx->bb.large_count, 0, 2 * sizeof(uint32_t), s));
+    if ((st = apply_resets(ctx, true)) != SLOTH_OK) return st;
     // indexed meshes share vertices: transformed once by the vertex kernel; soups in setup
     const float4 *tv = mesh->idx ? ctx->tv : nullptr;
     if (tv) CU(ctx, timed(ctx, "vertex", [&] { return launch_vertex_transform(md, M, ctx->tv, s); }));
@@ -764,9 +790,12 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     CU(ctx, timed(ctx, "newline", [&] { return launch_newline(mesh->ntri, ctx->tri_base, g, ctx->fb, s); }));
     CU(ctx, timed(ctx, "bin_count_large",[&] { return launch_bin_count_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
+    // the entry count comes back on a side stream, so that the draw's stream goes on
+    CU(ctx, cudaEventRecord(ctx->scan_ev, s));
+    CU(ctx, cudaStreamWaitEvent(ctx->side, ctx->scan_ev, 0));
     CU(ctx, cudaMemcpyAsync(ctx->h_total, ctx->bb.tile_offset + ntiles, sizeof(uint32_t),
-                            cudaMemcpyDeviceToHost, s));
-    CU(ctx, cudaEventRecord(ctx->total_ev, s));
+                            cudaMemcpyDeviceToHost, ctx->side));
+    CU(ctx, cudaEventRecord(ctx->total_ev, ctx->side));
     // The entry count sizes the entry buffer.  With a buffer from earlier draws the rest of
     // the draw goes ahead with it while the host waits for the count: the fill kernels
     // write no slot past the capacity and the raster does nothing when the count is above

@@ -90,6 +90,11 @@ struct Mat4 {
     float m[16];             // row-major
 };
 
+// frame resets (error word, fragments, newline tree) and draw resets (tile counts, large
+// queue counters), either or both, in one launch.
+cudaError_t launch_frame_reset(const FrameBuffers &fb, const BinBuffers &bb, uint32_t nl_nodes, uint32_t ntiles,
+                               bool frame, bool draw, cudaStream_t s);
+
 // vertex transform: tv[i] = (M*v_i).xyz (nalgebra order), float4 per vertex.
 cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *tv,
                                     cudaStream_t s);
