@@ -763,7 +763,7 @@ def main():
     ap.add_argument("--no-depth-cull", action="store_true",
                     help="rasterize every triangle (SLOTH_OPTION_DEPTH_CULL 0)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
-    ap.add_argument("--e2e-contexts", type=int, default=4, help="contexts (one host thread each) in the end-to-end leg")
+    ap.add_argument("--e2e-contexts", type=int, default=6, help="contexts (one host thread each) in the end-to-end leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched config-3 leg")
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable legs (configs 4 and 5)")
