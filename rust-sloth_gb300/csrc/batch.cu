@@ -72,8 +72,8 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_setup_kernel(BatchDev 
         const float4 *tv = b.tv + d.vert_off;
         r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), d.mesh.rgb + 3 * (size_t)t, f.g.w,
                          f.g.h);
-        f.fb.records[d.local_base + t] = r;
         sp = tile_span(vp, r);
+        store_record(f.fb.records + d.local_base + t, r, sp.ntiles);
         large = sp.large;
     }
     count_small_tiles_warp(live && !large, r, vp, sp, b.bb.tile_count + f.tile_off);

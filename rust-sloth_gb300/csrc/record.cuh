@@ -69,6 +69,15 @@ __device__ __forceinline__ int sat_hi(float f)
     return f > 0.0f ? (int)f : 0;
 }
 
+// Stores a record.  A triangle with no tile (culled, empty sample range) only ever has its
+// sample range read -- by the newline and fill kernels, which stop there -- so only that
+// row is written.
+__device__ __forceinline__ void store_record(TriRecord *dst, const TriRecord &r, uint32_t ntiles)
+{
+    if (ntiles != 0) *dst = r;
+    else reinterpret_cast<int4 *>(dst)[4] = make_int4(r.x0, r.xe, r.y0, r.y1);
+}
+
 // The record of one triangle with transformed vertices p1, p2, p3 (xyz) and face colour
 // c[0..2] in a w x h context.
 __device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p3, const uint8_t *c,

@@ -83,8 +83,8 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
         else
             r = build_record(transform_vertex(mesh, M, i1), transform_vertex(mesh, M, i2),
                              transform_vertex(mesh, M, i3), mesh.rgb + 3 * (size_t)t, g.w, g.h);
-        fb.records[tri_base + t] = r;
         sp = tile_span(vp, r);
+        store_record(fb.records + tri_base + t, r, sp.ntiles);
         large = sp.large;
     }
     // binning: count tiles of small triangles here, queue the rest for warps
