@@ -201,12 +201,13 @@ bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, 
     TriRecord r;
     TileSpan sp{};
     if (live) {
-        // the sample range first: culled and off-screen triangles end here
-        const int4 xr = __ldg(reinterpret_cast<const int4 *>(fb.records + gtri) + 4);
-        if (xr.x < xr.y && xr.z < xr.w) {
-            r = fb.records[gtri];
-            sp = tile_span(vp, r);
-        }
+        // the whole record in one round trip (a triangle without tiles has only its
+        // sample range stored, and nothing else of it is used)
+        const float4 *p = reinterpret_cast<const float4 *>(fb.records + gtri);
+        float4 *o = reinterpret_cast<float4 *>(&r);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) o[k] = __ldg(p + k);
+        sp = tile_span(vp, r);
     }
     fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
 }
