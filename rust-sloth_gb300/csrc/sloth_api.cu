@@ -80,6 +80,9 @@ struct sloth_ctx {
     bool reset_pending = false;    // a clear's resets, folded into the next launch that needs them
     cudaStream_t side = nullptr;   // the entry-count copy, off the draw's stream
     cudaEvent_t scan_ev = nullptr;
+    cudaStream_t nl_stream = nullptr;   // the newline fold, beside the binning kernels
+    cudaEvent_t setup_ev = nullptr, nl_ev = nullptr;
+    bool nl_pending = false;            // a newline fold not yet joined into the ctx stream
 
     // instrumentation
     int depth_cull = 1;
@@ -135,10 +138,11 @@ static void dfree(T *&p)
     p = nullptr;
 }
 
-// Time one launch on the ctx stream when timing is enabled.
+// Time one launch on stream s (default: the ctx stream) when timing is enabled.
 template <class F>
-static cudaError_t timed(sloth_ctx *ctx, const char *name, F &&launch)
+static cudaError_t timed(sloth_ctx *ctx, const char *name, F &&launch, cudaStream_t s = nullptr)
 {
+    if (!s) s = ctx->stream;
     if (!ctx->timing) {
         cudaError_t e = launch();
         if (e == cudaSuccess) ctx->launches++;
@@ -147,9 +151,9 @@ static cudaError_t timed(sloth_ctx *ctx, const char *name, F &&launch)
     EventPair ev;
     cudaEventCreate(&ev.a);
     cudaEventCreate(&ev.b);
-    cudaEventRecord(ev.a, ctx->stream);
+    cudaEventRecord(ev.a, s);
     cudaError_t e = launch();
-    cudaEventRecord(ev.b, ctx->stream);
+    cudaEventRecord(ev.b, s);
     if (e == cudaSuccess) {
         ctx->launches++;
         ctx->clocks[name].pending.push_back(ev);
@@ -160,8 +164,18 @@ static cudaError_t timed(sloth_ctx *ctx, const char *name, F &&launch)
     return e;
 }
 
+// Waits for the context's helper streams (newline fold, entry-count copy) before device
+// memory they may read is released.
+static void quiesce_helpers(sloth_ctx *ctx)
+{
+    if (ctx->nl_stream) cudaStreamSynchronize(ctx->nl_stream);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    ctx->nl_pending = false;
+}
+
 static void free_frame(sloth_ctx *ctx)
 {
+    quiesce_helpers(ctx);
     dfree(ctx->fb.keys);
     dfree(ctx->fb.tile_gen);
     dfree(ctx->fb.nltree);
@@ -225,6 +239,7 @@ static sloth_status ensure_records(sloth_ctx *ctx, size_t need)
         CU(ctx, cudaMemcpyAsync(n, ctx->fb.records, (size_t)ctx->tri_base * sizeof(TriRecord),
                                 cudaMemcpyDeviceToDevice, ctx->stream));
     CU(ctx, cudaStreamSynchronize(ctx->stream));
+    quiesce_helpers(ctx);
     dfree(ctx->fb.records);
     ctx->fb.records = n;
     ctx->records_cap = cap;
@@ -238,6 +253,7 @@ static sloth_status ensure_scratch(sloth_ctx *ctx, T **p, size_t *cap, size_t ne
     size_t c = *cap ? *cap : 1024;
     while (c < need) c *= 2;
     CU(ctx, cudaStreamSynchronize(ctx->stream));
+    quiesce_helpers(ctx);
     dfree(*p);
     CU(ctx, dalloc(p, c));
     *cap = c;
@@ -275,12 +291,22 @@ static sloth_status report_device_error(sloth_ctx *ctx)
     return SLOTH_OK;
 }
 
+// The ctx stream waits for the last newline fold (before a resolve or the next draw).
+static sloth_status join_newline(sloth_ctx *ctx)
+{
+    if (!ctx->nl_pending) return SLOTH_OK;
+    CU(ctx, cudaStreamWaitEvent(ctx->stream, ctx->nl_ev, 0));
+    ctx->nl_pending = false;
+    return SLOTH_OK;
+}
+
 static sloth_status resolve_pending(sloth_ctx *ctx)
 {
     if (!ctx->have_frame)
         return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "the context has no frame: call sloth_ctx_clear first");
     sloth_status st0 = apply_resets(ctx, false);
     if (st0 != SLOTH_OK) return st0;
+    if ((st0 = join_newline(ctx)) != SLOTH_OK) return st0;
     if (!ctx->dirty) return SLOTH_OK;
     CU(ctx, timed(ctx, "resolve", [&] { return launch_resolve(ctx->g, ctx->fb, ctx->stream); }));
     ctx->dirty = false;
@@ -415,6 +441,9 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
         cudaEventCreateWithFlags(&ctx->total_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->scan_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->nl_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->setup_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->nl_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost(&ctx->h_frags, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMallocHost(&ctx->h_error, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->fb.error, sizeof(uint32_t)) != cudaSuccess ||
@@ -423,6 +452,9 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
         if (ctx->total_ev) cudaEventDestroy(ctx->total_ev);
         if (ctx->scan_ev) cudaEventDestroy(ctx->scan_ev);
         if (ctx->side) cudaStreamDestroy(ctx->side);
+        if (ctx->nl_stream) cudaStreamDestroy(ctx->nl_stream);
+        if (ctx->setup_ev) cudaEventDestroy(ctx->setup_ev);
+        if (ctx->nl_ev) cudaEventDestroy(ctx->nl_ev);
         if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
         if (ctx->h_error) cudaFreeHost(ctx->h_error);
         if (ctx->fb.error) cudaFree(ctx->fb.error);
@@ -440,6 +472,7 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    quiesce_helpers(ctx);
     // batches lose their device memory and meshes their context; destroying either
     // afterwards only frees what is left
     for (sloth_batch *b : ctx->batches) sloth_batch_detach(b);
@@ -460,6 +493,9 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     if (ctx->total_ev) cudaEventDestroy(ctx->total_ev);
     if (ctx->scan_ev) cudaEventDestroy(ctx->scan_ev);
     if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->nl_stream) cudaStreamDestroy(ctx->nl_stream);
+    if (ctx->setup_ev) cudaEventDestroy(ctx->setup_ev);
+    if (ctx->nl_ev) cudaEventDestroy(ctx->nl_ev);
     if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
     if (ctx->h_error) cudaFreeHost(ctx->h_error);
     dfree(ctx->fb.error);
@@ -782,12 +818,20 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     const FrameGeom &g = ctx->g;
     const uint32_t ntiles = (uint32_t)(g.ntx * g.nty);
     cudaStream_t s = ctx->stream;
+    if ((st = join_newline(ctx)) != SLOTH_OK) return st;
     if ((st = apply_resets(ctx, true)) != SLOTH_OK) return st;
     // indexed meshes share vertices: transformed once by the vertex kernel; soups in setup
     const float4 *tv = mesh->idx ? ctx->tv : nullptr;
     if (tv) CU(ctx, timed(ctx, "vertex", [&] { return launch_vertex_transform(md, M, ctx->tv, s); }));
     CU(ctx, timed(ctx, "setup", [&] { return launch_setup(md, tv, M, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
-    CU(ctx, timed(ctx, "newline", [&] { return launch_newline(mesh->ntri, ctx->tri_base, g, ctx->fb, s); }));
+    // the newline fold reads the records and feeds only the resolve: on its own stream,
+    // beside the binning kernels
+    CU(ctx, cudaEventRecord(ctx->setup_ev, s));
+    CU(ctx, cudaStreamWaitEvent(ctx->nl_stream, ctx->setup_ev, 0));
+    CU(ctx, timed(ctx, "newline", [&] { return launch_newline(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->nl_stream); },
+                  ctx->nl_stream));
+    CU(ctx, cudaEventRecord(ctx->nl_ev, ctx->nl_stream));
+    ctx->nl_pending = true;
     CU(ctx, timed(ctx, "bin_count_large",[&] { return launch_bin_count_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
     // the entry count comes back on a side stream, so that the draw's stream goes on
