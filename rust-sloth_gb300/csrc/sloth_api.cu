@@ -81,6 +81,8 @@ struct sloth_ctx {
     cudaStream_t side = nullptr;   // the entry-count copy, off the draw's stream
     cudaEvent_t scan_ev = nullptr;
     cudaStream_t nl_stream = nullptr;   // the newline fold, beside the binning kernels
+    cudaStream_t aux = nullptr;         // the large-triangle fill, beside the small one
+    cudaEvent_t fill_ev = nullptr, aux_ev = nullptr;
     cudaEvent_t setup_ev = nullptr, nl_ev = nullptr;
     bool nl_pending = false;            // a newline fold not yet joined into the ctx stream
 
@@ -169,6 +171,7 @@ static cudaError_t timed(sloth_ctx *ctx, const char *name, F &&launch, cudaStrea
 static void quiesce_helpers(sloth_ctx *ctx)
 {
     if (ctx->nl_stream) cudaStreamSynchronize(ctx->nl_stream);
+    if (ctx->aux) cudaStreamSynchronize(ctx->aux);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
     ctx->nl_pending = false;
 }
@@ -442,6 +445,9 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
         cudaEventCreateWithFlags(&ctx->scan_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->nl_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->fill_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->aux_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->setup_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->nl_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost(&ctx->h_frags, sizeof(unsigned long long)) != cudaSuccess ||
@@ -453,8 +459,11 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
         if (ctx->scan_ev) cudaEventDestroy(ctx->scan_ev);
         if (ctx->side) cudaStreamDestroy(ctx->side);
         if (ctx->nl_stream) cudaStreamDestroy(ctx->nl_stream);
+        if (ctx->aux) cudaStreamDestroy(ctx->aux);
         if (ctx->setup_ev) cudaEventDestroy(ctx->setup_ev);
         if (ctx->nl_ev) cudaEventDestroy(ctx->nl_ev);
+        if (ctx->fill_ev) cudaEventDestroy(ctx->fill_ev);
+        if (ctx->aux_ev) cudaEventDestroy(ctx->aux_ev);
         if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
         if (ctx->h_error) cudaFreeHost(ctx->h_error);
         if (ctx->fb.error) cudaFree(ctx->fb.error);
@@ -494,8 +503,11 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     if (ctx->scan_ev) cudaEventDestroy(ctx->scan_ev);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->nl_stream) cudaStreamDestroy(ctx->nl_stream);
+    if (ctx->aux) cudaStreamDestroy(ctx->aux);
     if (ctx->setup_ev) cudaEventDestroy(ctx->setup_ev);
     if (ctx->nl_ev) cudaEventDestroy(ctx->nl_ev);
+    if (ctx->fill_ev) cudaEventDestroy(ctx->fill_ev);
+    if (ctx->aux_ev) cudaEventDestroy(ctx->aux_ev);
     if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
     if (ctx->h_error) cudaFreeHost(ctx->h_error);
     dfree(ctx->fb.error);
@@ -846,8 +858,15 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     // it.  Only then does the host grow the buffer and run the rest again, after a scan
     // that resets the cursors.
     auto rest = [&](size_t entries_bound) -> sloth_status {
+        // the small and the large fill take slots from the same cursors (atomics): they
+        // run side by side, the large one on the aux stream
+        CU(ctx, cudaEventRecord(ctx->fill_ev, s));
+        CU(ctx, cudaStreamWaitEvent(ctx->aux, ctx->fill_ev, 0));
+        CU(ctx, timed(ctx, "bin_fill_large", [&] { return launch_bin_fill_large(ctx->tri_base, g, ctx->fb, ctx->bb, ctx->aux); },
+                      ctx->aux));
+        CU(ctx, cudaEventRecord(ctx->aux_ev, ctx->aux));
         CU(ctx, timed(ctx, "bin_fill", [&] { return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
-        CU(ctx, timed(ctx, "bin_fill_large", [&] { return launch_bin_fill_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+        CU(ctx, cudaStreamWaitEvent(s, ctx->aux_ev, 0));
         size_t icap = ctx->bb.item_capacity;
         sloth_status st2;
         if ((st2 = ensure_scratch(ctx, &ctx->bb.items, &icap, raster_item_bound(ntiles, entries_bound))) != SLOTH_OK)
