@@ -64,6 +64,10 @@ struct sloth_batch {
 
     cudaGraphExec_t graph = nullptr;
     bool rendered = false;
+    // side branches of a render: the newline fold (beside the binning) and the
+    // large-triangle fill (beside the small one), forked from and joined into `stream`
+    cudaStream_t nl_s = nullptr, aux_s = nullptr;
+    cudaEvent_t ev_setup = nullptr, ev_nl = nullptr, ev_fill = nullptr, ev_aux = nullptr;
 
     // differentiable shading
     int2 *diff_blk = nullptr;                 // (frame, first depth cell) per kDiffChunk
@@ -325,7 +329,10 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
         return e;
     if ((e = launch_batch_vertex(d, b->blk[0], b->nblk[0], s))) return e;
     if ((e = launch_batch_setup(d, b->blk[1], b->nblk[1], s))) return e;
-    if ((e = launch_batch_newline(d, b->blk[2], b->nblk[2], b->max_nl, s))) return e;
+    if ((e = cudaEventRecord(b->ev_setup, s))) return e;
+    if ((e = cudaStreamWaitEvent(b->nl_s, b->ev_setup, 0))) return e;
+    if ((e = launch_batch_newline(d, b->blk[2], b->nblk[2], b->max_nl, b->nl_s))) return e;
+    if ((e = cudaEventRecord(b->ev_nl, b->nl_s))) return e;
     if ((e = launch_batch_bin_large(d, false, s))) return e;
     return launch_bin_scan(b->total_tiles, d.bb, s);
 }
@@ -334,11 +341,16 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
 cudaError_t enqueue_back(sloth_batch *b, const BatchDev &d, cudaStream_t s)
 {
     cudaError_t e;
+    if ((e = cudaEventRecord(b->ev_fill, s))) return e;
+    if ((e = cudaStreamWaitEvent(b->aux_s, b->ev_fill, 0))) return e;
+    if ((e = launch_batch_bin_large(d, true, b->aux_s))) return e;
+    if ((e = cudaEventRecord(b->ev_aux, b->aux_s))) return e;
     if ((e = launch_batch_fill(d, b->blk[1], b->nblk[1], s))) return e;
-    if ((e = launch_batch_bin_large(d, true, s))) return e;
+    if ((e = cudaStreamWaitEvent(s, b->ev_aux, 0))) return e;
     if ((e = launch_batch_items(d, s))) return e;
     const int tw = kTileShapes[b->shape][0], th = kTileShapes[b->shape][1];
     if ((e = launch_batch_raster(d, tw, th, s))) return e;
+    if ((e = cudaStreamWaitEvent(s, b->ev_nl, 0))) return e;   // the newline tree is complete
     return launch_batch_resolve(d, b->blk[3], b->nblk[3], s);
 }
 
@@ -439,6 +451,8 @@ void sloth_batch_detach(sloth_batch *b)
     if (!b->ctx) return;
     cudaSetDevice(b->device);
     cudaStreamSynchronize(b->stream);
+    if (b->nl_s) cudaStreamSynchronize(b->nl_s);
+    if (b->aux_s) cudaStreamSynchronize(b->aux_s);
     free_layout(b);
     bfree(b->diff_blk);
     bfree(b->vis);
@@ -448,6 +462,16 @@ void sloth_batch_detach(sloth_batch *b)
     if (b->h_overflow) cudaFreeHost(b->h_overflow);
     if (b->h_error) cudaFreeHost(b->h_error);
     bfree(b->error);
+    for (cudaEvent_t *ev : {&b->ev_setup, &b->ev_nl, &b->ev_fill, &b->ev_aux})
+        if (*ev) {
+            cudaEventDestroy(*ev);
+            *ev = nullptr;
+        }
+    for (cudaStream_t *st : {&b->nl_s, &b->aux_s})
+        if (*st) {
+            cudaStreamDestroy(*st);
+            *st = nullptr;
+        }
     b->h_mats = nullptr;
     b->h_total = b->h_overflow = b->h_error = nullptr;
     b->ctx = nullptr;
@@ -493,6 +517,12 @@ sloth_status sloth_batch_create(sloth_ctx *ctx, const sloth_frame_desc *frames, 
         cudaMallocHost(&b->h_total, 4) != cudaSuccess || cudaMallocHost(&b->h_overflow, 4) != cudaSuccess ||
         cudaMallocHost(&b->h_error, 4) != cudaSuccess || cudaMalloc(&b->error, 4) != cudaSuccess ||
         cudaMemset(b->error, 0, 4) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->nl_s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->aux_s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_setup, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_nl, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fill, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_aux, cudaEventDisableTiming) != cudaSuccess ||
         prepare_batch_kernels() != cudaSuccess) {
         sloth_batch_detach(b);
         delete b;
