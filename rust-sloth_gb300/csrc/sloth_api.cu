@@ -268,8 +268,11 @@ static sloth_status ensure_scratch(sloth_ctx *ctx, T **p, size_t *cap, size_t ne
 static sloth_status apply_resets(sloth_ctx *ctx, bool draw)
 {
     if (!ctx->reset_pending && !draw) return SLOTH_OK;
-    CU(ctx, launch_frame_reset(ctx->fb, ctx->bb, 2u * (uint32_t)ctx->g.nl_size, (uint32_t)(ctx->g.ntx * ctx->g.nty),
-                               ctx->reset_pending, draw, ctx->stream));
+    const bool frame = ctx->reset_pending;
+    CU(ctx, timed(ctx, "reset", [&] {
+           return launch_frame_reset(ctx->fb, ctx->bb, 2u * (uint32_t)ctx->g.nl_size,
+                                     (uint32_t)(ctx->g.ntx * ctx->g.nty), frame, draw, ctx->stream);
+       }));
     ctx->reset_pending = false;
     return SLOTH_OK;
 }
