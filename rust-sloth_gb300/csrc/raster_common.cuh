@@ -91,10 +91,12 @@ __device__ __forceinline__ void bulk_store(void *gdst, const void *ssrc, uint32_
                  : "memory");
 }
 
-// Waits until every bulk store of the thread has completed (writes done, smem free).
+// Waits until every bulk store of the thread has read its shared-memory source, so that
+// the block may leave; the global writes complete by the end of the grid, before any
+// later kernel reads the keys (nothing in this grid reads a tile another block stores).
 __device__ __forceinline__ void bulk_store_drain()
 {
-    asm volatile("cp.async.bulk.commit_group;\ncp.async.bulk.wait_group 0;" ::: "memory");
+    asm volatile("cp.async.bulk.commit_group;\ncp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
 // Orders this thread's generic-proxy shared-memory writes before later async-proxy
