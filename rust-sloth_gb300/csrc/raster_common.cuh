@@ -168,7 +168,7 @@ __device__ __forceinline__ void edge_row_span(float dx, float dy, float ax, floa
 
 // Parts of more samples than this are walked over their rows' column spans; smaller ones
 // over the whole rectangle.
-constexpr int kSpanMinSamples = 64;
+constexpr int kSpanMinSamples = 128;
 
 // Walk the samples of rect c and fold covered samples' keys.  Large parts of records with
 // kFlagFiniteXY: lane i bounds row c.ya + i to the columns that can pass all three edges
@@ -264,7 +264,7 @@ __device__ __forceinline__ void raster_serial(const TriRecord &r, uint32_t gtri,
 
 // Entries whose clipped rectangles hold at most this many samples are walked by their
 // lane alone; larger ones by the whole warp.
-constexpr int kSerialMaxSamples = 16;
+constexpr int kSerialMaxSamples = 4;
 
 // Depth bounds: zmax_u / zmax_w are upper bounds of the farthest depth (ordered high key
 // word) among the tile's cells that unwrapped samples can write (row y in [1,h-2], column
@@ -460,9 +460,9 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         constexpr uint32_t kSlots = kRasterThreads / 32;
         uint32_t wb = 0;          // warp-uniform: the bucket of the current window's first entry
         // warp-uniform count of warp walks since the warp's last refresh of the bound: one
-        // refresh per 16 walks of a warp (culled entries do not count), warp w's first
-        // after 2 + 2w walks
-        uint32_t since = 14u - 2u * (uint32_t)wid;
+        // refresh per 8 walks of a warp (culled entries do not count), warp w's first
+        // after 1 + w walks
+        uint32_t since = 7u - (uint32_t)wid;
         for (;;) {
             uint32_t claim = 0;
             if (lane == 0) claim = atomicAdd(&S.next, 1u);
@@ -505,7 +505,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
             unsigned coop = __ballot_sync(0xffffffffu, live && !serial);
             while (coop) {
                 if (depth_cull) {
-                    if (since >= 16) {
+                    if (since >= 8) {
                         refresh_bounds<TW, TH>(S, R0, C0, g, lane);
                         since = 0;
                     }
