@@ -31,7 +31,7 @@ __device__ __forceinline__ void block_sync()
 
 constexpr float kFltMax = 3.40282347e+38f;
 constexpr uint64_t kEmptyKey = ~0ull;
-constexpr uint32_t kSmallMaxTilesDev = 8;   // triangles over more tiles are binned by warps
+constexpr uint32_t kSmallMaxTilesDev = 16;   // triangles over more tiles are binned by warps
 
 // orient(a, b, p) of src/rasterizer.rs:30-32 with the edge constants precomputed:
 // (bx-ax)*(py-ay) - (by-ay)*(px-ax) where dx = bx-ax, dy = by-ay.
