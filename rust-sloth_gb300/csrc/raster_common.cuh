@@ -263,8 +263,12 @@ __device__ __forceinline__ void raster_serial(const TriRecord &r, uint32_t gtri,
 }
 
 // Entries whose clipped rectangles hold at most this many samples are walked by their
-// lane alone; larger ones by the whole warp.
+// lane alone; larger ones by the whole warp.  When most of a warp's window is small
+// (meshes of tiny triangles), the lanes also take entries of up to kSerialWideSamples,
+// each lane busy with its own; otherwise a lane walking one alone would hold its warp's
+// walks of the large ones back.
 constexpr int kSerialMaxSamples = 4;
+constexpr int kSerialWideSamples = 16;
 
 // Depth bounds: zmax_u / zmax_w are upper bounds of the farthest depth (ordered high key
 // word) among the tile's cells that unwrapped samples can write (row y in [1,h-2], column
@@ -495,7 +499,8 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                 if (!U.empty()) area += rect_area(clip_unwrapped(vp, U, tr, tc));
                 if (!W.empty()) area += rect_area(clip_wrapped(vp, W, tr, tc));
             }
-            const bool serial = live && area <= kSerialMaxSamples;
+            const int small = __popc(__ballot_sync(0xffffffffu, live && area <= kSerialWideSamples));
+            const bool serial = live && area <= (small >= 16 ? kSerialWideSamples : kSerialMaxSamples);
             if (serial) {
                 const TriRecord r = load_record(fb.records, gtri);
                 const uint32_t zb = depth_cull ? (uint32_t)(ent >> 32) : 0u;
