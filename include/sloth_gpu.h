@@ -81,10 +81,14 @@ void sloth_viewport_transform(uint16_t width, uint16_t height, float extent, flo
 
 /* ---- context (src/context.rs:12-49) ------------------------------------------------- */
 
-/* Create a context on CUDA device `device`.  `stream` is a cudaStream_t to issue all
- * work on, or NULL for a library-owned stream.  The context starts blank like
- * Context::blank(image=false) (src/context.rs:22-34): 0x0 viewport, identity
- * utransform. */
+/* Create a context on CUDA device `device`.  `stream` is a cudaStream_t to order all
+ * work on, or NULL for a library-owned stream: a draw forks two kernels onto the
+ * context's own helper streams (the newline fold, the large-triangle fill) and joins
+ * them back into `stream` before the draw's raster, the resolve, the next draw and
+ * sloth_ctx_synchronize, so results read from `stream` are complete.  The context starts
+ * blank like Context::blank(image=false) (src/context.rs:22-34): 0x0 viewport, identity
+ * utransform.  Contexts are independent: different host threads may drive different
+ * contexts at once. */
 sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream);
 /* Destroys the context.  Batches made on it lose their device memory; they and the
  * context's meshes stay valid handles only for sloth_batch_destroy / sloth_mesh_destroy

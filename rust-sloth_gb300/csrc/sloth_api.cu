@@ -3,8 +3,9 @@
 // Host-side restatement of the reference's per-frame driver around the hot path:
 // Context::blank/update/clear (src/context.rs:22-45, 93-141), draw_mesh
 // (src/rasterizer.rs:39-46) and the buffer reads that Context::flush prints.  All device
-// memory is owned here; all work is issued on the context's stream.  There is no CPU
-// fallback: if CUDA or the kernels are unavailable every call fails with SLOTH_ERR_CUDA.
+// memory is owned here; all work is ordered on the context's stream (two kernels of a
+// draw run on helper streams forked from it and joined back).  There is no CPU fallback:
+// if CUDA or the kernels are unavailable every call fails with SLOTH_ERR_CUDA.
 //
 // Host float math below must be compiled with -ffp-contract=off (see build.py).
 #include "sloth_gpu.h"
@@ -670,6 +671,7 @@ sloth_status sloth_ctx_synchronize(sloth_ctx *ctx)
     CU(ctx, cudaSetDevice(ctx->device));
     sloth_status st = queue_error_copy(ctx);
     if (st != SLOTH_OK) return st;
+    if ((st = join_newline(ctx)) != SLOTH_OK) return st;   // every kernel of the context is done
     CU(ctx, cudaStreamSynchronize(ctx->stream));
     return report_device_error(ctx);
 }
