@@ -191,6 +191,42 @@ def time_oracle(m, R, U, fraction_den: int, threads: int, offset: int = 0) -> tu
     return time.perf_counter() - t0, n
 
 
+# ------------------------------------------------------------------------ parity checks
+def _same(gpu, ref) -> dict:
+    """Bit-exact comparison of one frame (cells, z bits, winners) with the oracle's."""
+    cells, z, winner = gpu
+    bc = int(np.count_nonzero(cells != ref.cells))
+    bz = int(np.count_nonzero(z.view(np.uint32) != ref.z.view(np.uint32)))
+    bw = int(np.count_nonzero(winner != ref.winner))
+    return {"bitexact": bc == 0 and bz == 0 and bw == 0, "cells_differ": bc, "depth_differ": bz,
+            "winners_differ": bw}
+
+
+def check_frames_vs_oracle(jobs, read_gpu, threads: int) -> dict:
+    """Renders every frame of `jobs` ((meshes, R, w, h, image, U) each) on the CPU oracle,
+    one frame per host thread at a time (the oracle's ctypes calls release the interpreter
+    lock), and compares it bit for bit with read_gpu(i) (cells, z, winner).  The GPU
+    frames are read in the calling thread, a window of frames at a time."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    bad, checked, cells = [], 0, 0
+    t0 = time.perf_counter()
+    win = max(1, 2 * threads)
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        for lo in range(0, len(jobs), win):
+            idx = list(range(lo, min(len(jobs), lo + win)))
+            refs = ex.map(lambda i: O.render(*jobs[i]), idx)
+            gpus = [read_gpu(i) for i in idx]
+            for i, g, r in zip(idx, gpus, refs):
+                res = _same(g, r)
+                checked += 1
+                cells += int(r.cells.size)
+                if not res["bitexact"]:
+                    bad.append({"frame": i, **res})
+    return {"frames_checked": checked, "frames_bitexact": checked - len(bad), "frame_cells_checked": cells,
+            "mismatches": bad[:8], "oracle_threads": threads, "seconds": time.perf_counter() - t0}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -212,6 +248,8 @@ def run_reference(args):
         times.append(t)
     tot = sum(times)
     fps = args.steps / (tot * den)
+    # one whole frame as well (not sampled), to state the sampled figure's error
+    t_full, _ = time_oracle(m, R, U, 1, threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot / args.steps,
@@ -222,6 +260,9 @@ def run_reference(args):
                          "sample": f"every {den}th triangle of the frame (1/{den} of the work) per step, "
                                    f"banded oracle on {threads} threads; frames/s = 1/(den * step time)"},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "full_frame": {"seconds": t_full, "frames_per_s": 1.0 / t_full,
+                       "sampled_over_full": fps * t_full,
+                       "note": "one whole frame (all 1,002,000 triangles) timed once after the sampled steps"},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -309,6 +350,20 @@ def run_gpu(args):
     ms = max_over_ranks([ms], dev, ws)[0]
     ms_per_step = ms / args.steps
     value = whole_job_rate(args.steps, ws, ms / 1000.0)
+
+    # ---- the last timed frame against the oracle at full size (outside the timed region)
+    parity = None
+    if not args.no_parity and rank == 0:
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        got = ctx.read()
+        ref = O.render([m], R, W_PX, H_PX, True, threads=threads)
+        parity = {"config2_full": {**_same(got, ref), "frame_cells": int(ref.cells.size),
+                                   "fragments_gpu": int(frags), "fragments_oracle": int(ref.fragments),
+                                   "oracle": f"banded oracle on {threads} threads",
+                                   "seconds": time.perf_counter() - t0}}
+        parity["config2_full"]["bitexact"] &= int(frags) == int(ref.fragments)
+        del ref, got
 
     # ---- end to end through the C ABI with host buffers
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -434,10 +489,15 @@ def run_gpu(args):
         cpu = {"value": 1.0 / (t * args.cpu_sample_den), "unit": "frames/s", "cores": 1, "kind": "port",
                "sample": f"every {args.cpu_sample_den}th triangle of the frame ({n} triangles, 1/{args.cpu_sample_den} "
                          f"of the work) on one thread in {t:.2f} s; frames/s = 1/(den * time)"}
+        if args.cpu_full_frame:
+            tf, _ = time_oracle(m, R, U, 1, 1)
+            cpu["full_frame"] = {"seconds": tf, "frames_per_s": 1.0 / tf, "sampled_over_full": cpu["value"] * tf}
 
     batched = None
     if not args.no_batched:
         batched = run_config3(torch, stream, local, args)
+        if parity is not None and "parity_vs_oracle" in batched:
+            parity["config3_frames"] = batched.pop("parity_vs_oracle")
     differentiable = inverse = None
     if not args.no_diff:
         differentiable = run_config4(torch, stream, local, args)
@@ -456,6 +516,7 @@ def run_gpu(args):
         "e2e": e2e,
         "gpu_launches": launches, "kernels": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
         "batched": batched, "differentiable": differentiable, "inverse_rendering": inverse,
+        "parity": parity,
     }
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -542,28 +603,20 @@ def run_config3(torch, stream, device, args):
     torch.cuda.synchronize()
     plain_ms = a.elapsed_time(b) / psteps
 
-    # the batched frames equal the plain ones bit for bit (spot check)
-    checked = 0
-    for i in (0, 17, 255, 256, len(frames) - 1):
-        f = frames[i]
-        key = (f["w"], f["h"], f["image"])
-        c = plain[key]
-        c.set_utransform(f["U"])
-        c.clear()
-        for m, R in f["draws"]:
-            c.draw_mesh(m, R)
-        pc, pz, pw = c.read()
-        bc, bz, bw = batch.read(i)
-        assert np.array_equal(pc, bc) and np.array_equal(pz.view(np.uint32), bz.view(np.uint32)) \
-            and np.array_equal(pw, bw), f"batched frame {i} differs from the plain path"
-        checked += 1
+    # every batched frame (the last timed render) against the oracle, bit for bit
+    par = None
+    if not args.no_parity:
+        jobs = [([meshes[mi]], R, w, h, im, U) for mi, w, h, im, U, R in specs]
+        par = check_frames_vs_oracle(jobs, batch.read, os.cpu_count() or 1)
     nframes = len(frames)
     out = {"workload": CONFIG3, "frames": nframes,
            "triangles": int(sum(m["rgb"].shape[0] for m in [meshes[s[0]] for s in specs])),
            "batched_frames_per_s": 1000.0 * nframes / batched_ms, "batched_ms_per_pass": batched_ms,
            "plain_frames_per_s": 1000.0 * nframes / plain_ms, "plain_ms_per_pass": plain_ms,
-           "batched_over_plain": plain_ms / batched_ms, "tile_shape": S.tile_shapes()[shape],
-           "bitexact_frames_checked": checked, "graph": True}
+           "batched_over_plain": plain_ms / batched_ms, "tile_shape": S.tile_shapes()[shape], "graph": True}
+    if par is not None:
+        out["bitexact_frames_vs_oracle"] = par["frames_bitexact"]
+        out["parity_vs_oracle"] = par
     for c in plain.values():
         c.close()
     batch.close()
@@ -760,9 +813,13 @@ def main():
     ap.add_argument("--cpu-sample-den", type=int, default=8)
     ap.add_argument("--ref-sample-den", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-full-frame", action="store_true",
+                    help="also time one whole config-2 frame on one thread (about a minute) beside the sample")
     ap.add_argument("--no-depth-cull", action="store_true",
                     help="rasterize every triangle (SLOTH_OPTION_DEPTH_CULL 0)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the full-size checks against the oracle (config 2 frame, every config-3 frame)")
     ap.add_argument("--e2e-contexts", type=int, default=6, help="contexts (one host thread each) in the end-to-end leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched config-3 leg")
     ap.add_argument("--batched-steps", type=int, default=20)

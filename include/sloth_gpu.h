@@ -316,11 +316,12 @@ sloth_status sloth_batch_shade_backward(sloth_batch *batch, const float *vertex_
  * until the process exits.  Limits: ntri <= SLOTH_NOALLOC_MAX_TRIANGLES,
  * height <= SLOTH_NOALLOC_MAX_HEIGHT, and the viewport padded to 64x32-cell tiles
  * ((ceil(w/64)*64) * (ceil(h/32)*32)) <= SLOTH_NOALLOC_MAX_DEPTH_CELLS; larger inputs
- * return SLOTH_ERR_LIMIT.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture.  All calls share the array, so calls that overlap on the GPU (on
- * different streams, or from different threads) race and corrupt each other's frames:
- * issue them one after another. */
+ * return SLOTH_ERR_LIMIT.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress, which allocates nothing) on the device the caller made current,
+ * so an address never outlives a cudaDeviceReset; the first call on a device also loads
+ * the library's kernels there, so make that first call before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU (on different streams, or from
+ * different threads) race and corrupt each other's frames: issue them one after another. */
 #define SLOTH_NOALLOC_MAX_TRIANGLES 32768u
 #define SLOTH_NOALLOC_MAX_HEIGHT 4096u
 #define SLOTH_NOALLOC_MAX_DEPTH_CELLS 524288u

@@ -80,6 +80,28 @@ MESHDUMP = OUT_DIR / "sloth_meshdump"
 HOST_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-I", str(INCLUDE)]
 
 
+def _meshdump_job(force: bool) -> list[str] | None:
+    dump_deps = [HOST / "meshdump.cpp", HOST / "loaders.cpp", HOST / "sloth_host.hpp", Path(__file__)]
+    if force or _stale(MESHDUMP, dump_deps):
+        # the loaders alone, no GPU library: usable where there is no CUDA device
+        return ["g++"] + HOST_FLAGS + [str(HOST / "meshdump.cpp"), str(HOST / "loaders.cpp"), "-o", str(MESHDUMP)]
+    return None
+
+
+def build_meshdump(force: bool = False, verbose: bool = False) -> Path:
+    """Compile `sloth_meshdump`, the C++ loaders without the GPU library (g++ only, a few
+    seconds); returns its path."""
+    OUT_DIR.mkdir(exist_ok=True)
+    job = _meshdump_job(force)
+    if job:
+        if verbose:
+            print(" ".join(job))
+        r = subprocess.run(job, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"meshdump build failed:\n{r.stdout}\n{r.stderr}")
+    return MESHDUMP
+
+
 def build_host(force: bool = False, verbose: bool = False) -> Path:
     """Compile the C++ host side (loaders, Context mirror, the `sloth` command) against
     libsloth_gpu.so; returns the command's path."""
@@ -89,11 +111,9 @@ def build_host(force: bool = False, verbose: bool = False) -> Path:
     if force or _stale(CLI, deps):
         jobs.append(["g++"] + HOST_FLAGS + [str(HOST / s) for s in HOST_SOURCES] + [
             "-o", str(CLI), "-L", str(OUT_DIR), "-lsloth_gpu", "-Wl,-rpath,$ORIGIN"])
-    dump_deps = [HOST / "meshdump.cpp", HOST / "loaders.cpp", HOST / "sloth_host.hpp", Path(__file__)]
-    if force or _stale(MESHDUMP, dump_deps):
-        # the loaders alone, no GPU library: usable where there is no CUDA device
-        jobs.append(["g++"] + HOST_FLAGS + [str(HOST / "meshdump.cpp"), str(HOST / "loaders.cpp"),
-                                            "-o", str(MESHDUMP)])
+    dump = _meshdump_job(force)
+    if dump:
+        jobs.append(dump)
     procs = [subprocess.Popen(c, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True) for c in jobs]
     for c, p in zip(jobs, procs):
         out, err = p.communicate()

@@ -266,8 +266,9 @@ cudaError_t launch_batch_newline(const BatchDev &b, const int2 *blocks, uint32_t
 
 cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s)
 {
-    if (fill) batch_bin_large_kernel<true><<<8 * 152, 256, 0, s>>>(b);
-    else batch_bin_large_kernel<false><<<8 * 152, 256, 0, s>>>(b);
+    const int grid = 8 * device_sm_count();   // eight CTAs of 8 warps per SM; the warps stride over the items
+    if (fill) batch_bin_large_kernel<true><<<grid, 256, 0, s>>>(b);
+    else batch_bin_large_kernel<false><<<grid, 256, 0, s>>>(b);
     return cudaGetLastError();
 }
 

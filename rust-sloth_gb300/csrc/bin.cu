@@ -214,7 +214,7 @@ bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, 
 
 static int large_grid()
 {
-    return 8 * 152;   // up to eight CTAs of 8 warps per SM; the warps stride over the items
+    return 8 * device_sm_count();   // up to eight CTAs of 8 warps per SM; the warps stride over the items
 }
 
 cudaError_t launch_bin_count_large(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,

@@ -19,8 +19,6 @@
 //   tile_gen  kMaxTiles x 4 B         tile generations (cleared every call)
 //   nltree    2*kMaxNl x 4 B          newline segment tree (cleared every call)
 //   frags     8 B                     fragment counter (cleared every call)
-#include <mutex>
-
 #include "sloth_gpu.h"
 #include "sloth_internal.cuh"
 #include "sloth_kernels.h"
@@ -50,7 +48,8 @@ static_assert(kScratchBytes == SLOTH_NOALLOC_SCRATCH_BYTES, "header states the s
 }  // namespace
 
 // The scratch every call uses.  In host code this name is only a stand-in for the
-// device symbol; its device address comes from cudaGetSymbolAddress (scratch_on()).
+// device symbol; its device address comes from cudaGetSymbolAddress (scratch_on()), with
+// the device the caller made current.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 // Raster variant without binning: one CTA per tile tests every triangle of the draw
@@ -123,22 +122,16 @@ noalloc_raster_kernel(uint32_t ntri, FrameGeom g, FrameBuffers fb)
 
 namespace {
 
-// Device address of g_noalloc_scratch on each device, looked up once per device with
-// that device current (the first call on a device does it).
-std::mutex g_scratch_mu;
-unsigned char *g_scratch_ptr[64] = {};
-
-cudaError_t scratch_on(int device, unsigned char **out)
+// Device address of g_noalloc_scratch for the current device, looked up on every call with
+// the caller's device current.  cudaGetSymbolAddress allocates nothing; an address kept
+// from an earlier call could belong to a context that cudaDeviceReset (or a driver-API
+// caller switching contexts) has since replaced, and kernels given it would fault.
+cudaError_t scratch_on(unsigned char **out)
 {
-    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[device]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_ptr[device] = static_cast<unsigned char *>(p);
-    }
-    *out = g_scratch_ptr[device];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    *out = static_cast<unsigned char *>(p);
     return cudaSuccess;
 }
 
@@ -172,10 +165,8 @@ extern "C" sloth_status sloth_render_noalloc(const float *x, const float *y, con
     if (padded > kMaxCells) return SLOTH_ERR_LIMIT;
     const uint32_t ntiles = (uint32_t)(g.ntx * g.nty);
 
-    int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess) return SLOTH_ERR_CUDA;
     unsigned char *base = nullptr;
-    if (scratch_on(device, &base) != cudaSuccess) return SLOTH_ERR_CUDA;
+    if (scratch_on(&base) != cudaSuccess) return SLOTH_ERR_CUDA;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     FrameBuffers fb{};

@@ -24,7 +24,8 @@ cudaError_t launch_resolve(const FrameGeom &g, const FrameBuffers &fb, cudaStrea
     const uint64_t ncells = (uint64_t)g.w * g.h + (g.image ? g.h : 0);
     if (ncells == 0) return cudaSuccess;
     uint64_t blocks = ((ncells + kRun - 1) / kRun + 255) / 256;
-    if (blocks > 152u * 32u) blocks = 152u * 32u;
+    const uint64_t cap = 32ull * (uint64_t)device_sm_count();   // eight resident CTAs per SM, four waves
+    if (blocks > cap) blocks = cap;
     const int vec = ((reinterpret_cast<uintptr_t>(fb.cells_out) | reinterpret_cast<uintptr_t>(fb.z_out) |
                       reinterpret_cast<uintptr_t>(fb.winner_out)) & (4u * kRun - 1u)) == 0;
     resolve_kernel<<<(unsigned)blocks, 256, 0, s>>>(g, fb, vec);

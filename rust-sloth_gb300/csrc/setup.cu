@@ -5,6 +5,8 @@
 // recomputes utransform*transform per triangle and normal() per covered sample; both
 // are the same value every time, so they are formed once (matrix on the host, normal
 // here) with the same operation order (record.cuh).
+#include <atomic>
+
 #include "bin_common.cuh"
 #include "record.cuh"
 #include "sloth_kernels.h"
@@ -170,6 +172,21 @@ cudaError_t launch_frame_reset(const FrameBuffers &fb, const BinBuffers &bb, uin
     const uint32_t n = max(frame ? nl_nodes : 1u, draw ? ntiles : 1u);
     frame_reset_kernel<<<(n + 255) / 256, 256, 0, s>>>(fb, bb, nl_nodes, ntiles, frame ? 1 : 0, draw ? 1 : 0);
     return cudaGetLastError();
+}
+
+int device_sm_count()
+{
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+    if (dev < 64) {
+        const int c = cache[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+    if (dev < 64) cache[dev].store(n, std::memory_order_relaxed);
+    return n;
 }
 
 cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *tv, cudaStream_t s)

@@ -90,6 +90,10 @@ struct Mat4 {
     float m[16];             // row-major
 };
 
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked
+// up once per device): grids of the grid-stride kernels are sized by it.
+int device_sm_count();
+
 // frame resets (error word, fragments, newline tree) and draw resets (tile counts, large
 // queue counters), either or both, in one launch.
 cudaError_t launch_frame_reset(const FrameBuffers &fb, const BinBuffers &bb, uint32_t nl_nodes, uint32_t ntiles,

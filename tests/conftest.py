@@ -21,5 +21,9 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session", autouse=True)
 def _oracle_built():
+    """The oracle and the GPU-free loader tool (`sloth_meshdump`) are built for every run,
+    so the loader tests never depend on an earlier build step."""
     from oracle.build import build_oracle
+    import build as pkg_build   # rust-sloth_gb300/build.py
     build_oracle()
+    pkg_build.build_meshdump()

@@ -2,7 +2,9 @@
 folder, what the Python restatement of its loaders (rust-sloth_gb300/workloads.py:
 read_obj, read_stl) reads -- per mesh the triangle count, a SHA-256 of the positions and
 colours, and the bounding box maximum -- or the error text.  Run where the reference tree
-is present:  python tests/golden/make_model_fixtures.py /root/reference/models"""
+is present:  python tests/golden/make_model_fixtures.py <reference checkout>/models
+(or with SLOTH_MODELS_DIR set)."""
+import os
 import json
 import sys
 from pathlib import Path
@@ -30,4 +32,7 @@ def main(models_dir: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/models")
+    d = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SLOTH_MODELS_DIR")
+    if not d:
+        sys.exit("usage: make_model_fixtures.py <models dir>  (or set SLOTH_MODELS_DIR)")
+    main(d)
