@@ -565,10 +565,11 @@ def run_config3(torch, stream, device, args):
     batch = S.Batch(ctx, frames)
     batch.render()
     if args.batched_shape >= 0:
-        shape = args.batched_shape
+        shape, direct = args.batched_shape, max(0, args.batched_direct)
         batch.set_tile_shape(shape)
+        batch.set_direct_samples(direct)
     else:
-        shape, _ = batch.autotune(reps=2)
+        shape, direct, _ = batch.autotune(reps=2)
     batch.render()
     torch.cuda.synchronize()
     steps = max(3, args.batched_steps)
@@ -613,7 +614,8 @@ def run_config3(torch, stream, device, args):
            "triangles": int(sum(m["rgb"].shape[0] for m in [meshes[s[0]] for s in specs])),
            "batched_frames_per_s": 1000.0 * nframes / batched_ms, "batched_ms_per_pass": batched_ms,
            "plain_frames_per_s": 1000.0 * nframes / plain_ms, "plain_ms_per_pass": plain_ms,
-           "batched_over_plain": plain_ms / batched_ms, "tile_shape": S.tile_shapes()[shape], "graph": True}
+           "batched_over_plain": plain_ms / batched_ms, "tile_shape": S.tile_shapes()[shape],
+           "direct_samples": direct, "graph": True}
     if par is not None:
         out["bitexact_frames_vs_oracle"] = par["frames_bitexact"]
         out["parity_vs_oracle"] = par
@@ -826,7 +828,9 @@ def main():
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable legs (configs 4 and 5)")
     ap.add_argument("--only-batched", action="store_true", help="run only the batched config-3 leg")
     ap.add_argument("--batched-shape", type=int, default=-1,
-                    help="tile shape of the config-3 batch (default: autotuned)")
+                    help="tile shape of the config-3 batch (default: autotuned with the direct limit)")
+    ap.add_argument("--batched-direct", type=int, default=0,
+                    help="direct-sample limit of the config-3 batch when --batched-shape fixes the shape")
     ap.add_argument("--only-diff", action="store_true", help="run only the differentiable legs (configs 4 and 5)")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     args = ap.parse_args()

@@ -174,6 +174,13 @@ sloth_status sloth_ctx_flush_device(sloth_ctx *ctx, int format, const char **dev
  *   SLOTH_ERR_DEVICE_FAULT (a clear starts the next frame without the error).  0 (the
  *   default) is normal operation. */
 #define SLOTH_OPTION_WAIT_TEST 3
+/* SLOTH_OPTION_DIRECT_SAMPLES: triangles whose sample range (after the exact tightening of
+ *   its right edge) holds at most this many samples are rasterized by the setup kernel
+ *   straight into the global depth keys (a 64-bit atomicMin per covered sample) instead of
+ *   being binned into tiles; 0 (the default) bins every triangle.  0..SLOTH_MAX_DIRECT_SAMPLES;
+ *   takes effect at the next sloth_ctx_clear.  Results are identical either way. */
+#define SLOTH_OPTION_DIRECT_SAMPLES 4
+#define SLOTH_MAX_DIRECT_SAMPLES 256
 sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value);
 
 /* The raster tile shapes the library is built for: shape i is `cells` depth cells wide
@@ -256,9 +263,13 @@ sloth_status sloth_batch_flush(sloth_batch *batch, uint32_t frame, int format, c
                                uint64_t *bytes);
 /* Use tile shape `shape` (sloth_tile_shape) for this batch; re-lays out its buffers. */
 sloth_status sloth_batch_set_tile_shape(sloth_batch *batch, int shape);
-/* Autotuner: render the batch `reps` times with every tile shape, keep the fastest;
- * reports the shape and its mean render time in ms. */
-sloth_status sloth_batch_autotune(sloth_batch *batch, int reps, int *best_shape, float *best_ms);
+/* Rasterize triangles of at most `samples` samples straight into the depth keys during
+ * setup (SLOTH_OPTION_DIRECT_SAMPLES for a batch; a new batch takes its context's value). */
+sloth_status sloth_batch_set_direct_samples(sloth_batch *batch, int samples);
+/* Autotuner: render the batch `reps` times with every tile shape and every candidate
+ * direct-sample limit (0, 4, 16, 64), keep the fastest pair; reports the pair and its mean
+ * render time in ms (any output may be NULL). */
+sloth_status sloth_batch_autotune(sloth_batch *batch, int reps, int *best_shape, int *best_direct, float *best_ms);
 
 /* ---- differentiable shading of a rendered batch ----------------------------------- */
 

@@ -5,6 +5,7 @@
 // item's frame, so each frame is bit-identical to drawing it alone.
 #include "batch_kernels.h"
 #include "bin_common.cuh"
+#include "direct.cuh"
 #include "raster_common.cuh"
 #include "record.cuh"
 #include "resolve_common.cuh"
@@ -55,7 +56,7 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_setup_kernel(BatchDev 
     const BatchDraw &d = b.draws[blk.x];
     const BatchFrame &f = b.frames[d.frame];
     const uint32_t t = (uint32_t)blk.y + threadIdx.x;
-    bool large = false;
+    bool large = false, direct = false;
     const bool live = t < d.mesh.ntri;
     TriRecord r;
     TileSpan sp{};
@@ -74,15 +75,23 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_setup_kernel(BatchDev 
                          f.g.h);
         sp = tile_span(vp, r);
         store_record(f.fb.records + d.local_base + t, r, sp.ntiles);
-        large = sp.large;
+        direct = is_direct(r.x0, r.xe, r.y0, r.y1, f.g.direct_max);
+        large = sp.large && !direct;
     }
-    count_small_tiles_warp(live && !large, r, vp, sp, b.bb.tile_count + f.tile_off);
+    count_small_tiles_warp(live && !large && !direct, r, vp, sp, b.bb.tile_count + f.tile_off);
     if (__any_sync(0xffffffffu, large)) {
         const int q = large_slot(large, sp.ntiles, b.bb.large_count, b.bb.large_cap);
         if (q >= 0) {
             b.bb.large_queue[q] = d.local_base + t;   // frame-local draw index
             b.large_frame[q] = d.frame;
         }
+    }
+    // the smallest triangles fold their samples into the frame's global keys (direct.cuh)
+    if (__any_sync(0xffffffffu, direct)) {
+        const uint32_t frags = direct ? direct_raster(r, d.local_base + t, f.g.w, f.g.pitch,
+                                                      reinterpret_cast<unsigned long long *>(f.fb.keys))
+                                      : 0u;
+        add_frags_warp(frags, f.fb.fragments);
     }
 }
 
@@ -149,7 +158,7 @@ __global__ void __launch_bounds__(kBatchSetupBlock) batch_fill_kernel(BatchDev b
     if (live) {
         // the sample range first: culled and off-screen triangles end here
         const int4 xr = __ldg(reinterpret_cast<const int4 *>(f.fb.records + gtri) + 4);
-        if (xr.x < xr.y && xr.z < xr.w) {
+        if (xr.x < xr.y && xr.z < xr.w && !is_direct(xr.x, xr.y, xr.z, xr.w, f.g.direct_max)) {
             r = f.fb.records[gtri];
             sp = tile_span(vp, r);
         }

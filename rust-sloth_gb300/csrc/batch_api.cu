@@ -20,6 +20,11 @@
 
 using namespace sloth;
 
+// Clear generation of every batch frame: each render clears the tile generations to 0 (no
+// tile current) or, when small triangles are folded straight into the keys, fills them
+// with the byte 0x01 (every tile current), so the value has 0x01 in every byte.
+constexpr uint32_t kBatchGen = 0x01010101u;
+
 struct sloth_batch {
     sloth_ctx *ctx = nullptr;
     int device = 0;
@@ -28,6 +33,7 @@ struct sloth_batch {
     std::vector<const sloth_mesh *> meshes;   // per draw
     std::vector<float> transforms;            // 16 per draw
     int shape = 0;
+    int direct_max = 0;                       // FrameGeom::direct_max of every frame
 
     // layout (per shape)
     std::vector<BatchFrame> hframes;
@@ -86,6 +92,7 @@ void sloth_ctx_unregister_batch(sloth_ctx *ctx, sloth_batch *b);
 int sloth_ctx_device(const sloth_ctx *ctx);
 cudaStream_t sloth_ctx_stream(const sloth_ctx *ctx);
 int sloth_ctx_depth_cull(const sloth_ctx *ctx);
+int sloth_ctx_direct_samples(const sloth_ctx *ctx);
 struct MeshView {
     const float *x, *y, *z;
     const uint32_t *idx;
@@ -195,6 +202,7 @@ sloth_status build(sloth_batch *b, int shape)
         g.pitch = g.ntx * tw;
         g.nl_size = 1;
         while (g.nl_size < g.h) g.nl_size <<= 1;
+        g.direct_max = b->direct_max;
         b->max_nl = g.nl_size > b->max_nl ? g.nl_size : b->max_nl;
         BatchFrame &bf = b->hframes[f];
         bf.g = g;
@@ -279,7 +287,7 @@ sloth_status build(sloth_batch *b, int shape)
         bf.fb.winner_out = b->winner + b->z_off[f];
         bf.fb.fragments = b->fragments;
         bf.fb.error = b->error;
-        bf.fb.gen = 1;
+        bf.fb.gen = kBatchGen;
     }
     BCU(b, balloc(&b->d_frames, nf));
     BCU(b, balloc(&b->d_draws, nd));
@@ -320,7 +328,14 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
 {
     cudaError_t e;
     if ((e = cudaMemsetAsync(b->bb.tile_count, 0, (size_t)b->total_tiles * 4, s))) return e;
-    if ((e = cudaMemsetAsync(b->tile_gen, 0, (size_t)b->total_tiles * 4, s))) return e;
+    if (b->direct_max > 0) {
+        // small triangles fold into the global keys during setup: every tile's keys start
+        // empty and current (kBatchGen is 0x01 in every byte)
+        if ((e = cudaMemsetAsync(b->keys, 0xff, (size_t)b->total_keys * 8, s))) return e;
+        if ((e = cudaMemsetAsync(b->tile_gen, 0x01, (size_t)b->total_tiles * 4, s))) return e;
+    } else {
+        if ((e = cudaMemsetAsync(b->tile_gen, 0, (size_t)b->total_tiles * 4, s))) return e;
+    }
     if ((e = cudaMemsetAsync(b->nltree, 0xff, (size_t)b->total_nl * 4, s))) return e;
     if ((e = cudaMemsetAsync(b->bb.large_count, 0, 8, s))) return e;
     if ((e = cudaMemsetAsync(b->fragments, 0, 8, s))) return e;
@@ -529,6 +544,7 @@ sloth_status sloth_batch_create(sloth_ctx *ctx, const sloth_frame_desc *frames, 
         return sloth_ctx_fail(ctx, SLOTH_ERR_OUT_OF_MEMORY, "batch host buffers");
     }
     sloth_ctx_register_batch(ctx, b);
+    b->direct_max = sloth_ctx_direct_samples(ctx);
     set_mats(b);
     const sloth_status st = build(b, 0);
     if (st != SLOTH_OK) {
@@ -642,7 +658,28 @@ sloth_status sloth_batch_set_tile_shape(sloth_batch *b, int shape)
     return shape == b->shape ? SLOTH_OK : build(b, shape);
 }
 
-sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, float *best_ms)
+sloth_status sloth_batch_set_direct_samples(sloth_batch *b, int samples)
+{
+    if (!b || !b->ctx || samples < 0 || samples > SLOTH_MAX_DIRECT_SAMPLES) return SLOTH_ERR_INVALID_ARGUMENT;
+    BCU(b, cudaSetDevice(b->device));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    if (samples == b->direct_max) return SLOTH_OK;
+    b->direct_max = samples;
+    for (BatchFrame &f : b->hframes) f.g.direct_max = samples;
+    if (b->d_frames)
+        BCU(b, cudaMemcpy(b->d_frames, b->hframes.data(), b->hframes.size() * sizeof(BatchFrame),
+                          cudaMemcpyHostToDevice));
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);   // the key clear of a render depends on the setting
+        b->graph = nullptr;
+    }
+    return SLOTH_OK;
+}
+
+// Candidate sample limits of the direct path the autotuner tries (0: every triangle binned).
+static const int kDirectCandidates[] = {0, 4, 16, 64};
+
+sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, int *best_direct, float *best_ms)
 {
     if (!b || !b->ctx) return SLOTH_ERR_INVALID_ARGUMENT;
     if (reps < 1) reps = 3;
@@ -650,35 +687,40 @@ sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, flo
     cudaEvent_t e0, e1;
     BCU(b, cudaEventCreate(&e0));
     BCU(b, cudaEventCreate(&e1));
-    int best = -1;
+    int best = -1, bestd = 0;
     float best_t = 0.0f;
-    for (int shape = 0; shape < kNumTileShapes; ++shape) {
-        sloth_status st = sloth_batch_set_tile_shape(b, shape);
-        if (st == SLOTH_OK) st = sloth_batch_render(b);     // plan + size the entries
-        if (st == SLOTH_OK) st = settle(b);
-        if (st == SLOTH_OK) st = sloth_batch_render(b);     // capture + warm
-        if (st != SLOTH_OK) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return st;
-        }
-        cudaEventRecord(e0, b->stream);
-        for (int i = 0; i < reps; ++i) sloth_batch_render(b);
-        cudaEventRecord(e1, b->stream);
-        cudaEventSynchronize(e1);
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        ms /= (float)reps;
-        if (best < 0 || ms < best_t) {
-            best = shape;
-            best_t = ms;
+    sloth_status st = SLOTH_OK;
+    for (int shape = 0; shape < kNumTileShapes && st == SLOTH_OK; ++shape) {
+        for (int dm : kDirectCandidates) {
+            st = sloth_batch_set_tile_shape(b, shape);
+            if (st == SLOTH_OK) st = sloth_batch_set_direct_samples(b, dm);
+            if (st == SLOTH_OK) st = sloth_batch_render(b);     // plan + size the entries
+            if (st == SLOTH_OK) st = settle(b);
+            if (st == SLOTH_OK) st = sloth_batch_render(b);     // capture + warm
+            if (st == SLOTH_OK) st = settle(b);
+            if (st != SLOTH_OK) break;
+            cudaEventRecord(e0, b->stream);
+            for (int i = 0; i < reps; ++i) sloth_batch_render(b);
+            cudaEventRecord(e1, b->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= (float)reps;
+            if (best < 0 || ms < best_t) {
+                best = shape;
+                bestd = dm;
+                best_t = ms;
+            }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    sloth_status st = sloth_batch_set_tile_shape(b, best);
+    if (st != SLOTH_OK) return st;
+    st = sloth_batch_set_tile_shape(b, best);
+    if (st == SLOTH_OK) st = sloth_batch_set_direct_samples(b, bestd);
     if (st != SLOTH_OK) return st;
     if (best_shape) *best_shape = best;
+    if (best_direct) *best_direct = bestd;
     if (best_ms) *best_ms = best_t;
     return SLOTH_OK;
 }

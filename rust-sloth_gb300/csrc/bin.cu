@@ -5,6 +5,7 @@
 // cells it can write: count (setup kernel for small triangles, one warp per large
 // triangle here), exclusive scan over tiles, then fill (bin_common.cuh).
 #include "bin_common.cuh"
+#include "direct.cuh"
 #include "sloth_kernels.h"
 
 namespace sloth {
@@ -208,6 +209,7 @@ bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, 
 #pragma unroll
         for (int k = 0; k < 6; ++k) o[k] = __ldg(p + k);
         sp = tile_span(vp, r);
+        if (is_direct(r.x0, r.xe, r.y0, r.y1, g.direct_max)) sp.ntiles = 0;   // rasterized by setup
     }
     fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
 }

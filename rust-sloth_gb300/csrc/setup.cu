@@ -8,6 +8,7 @@
 #include <atomic>
 
 #include "bin_common.cuh"
+#include "direct.cuh"
 #include "record.cuh"
 #include "sloth_kernels.h"
 
@@ -67,7 +68,7 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = t < mesh.ntri;
-    bool large = false;
+    bool large = false, direct = false;
     TriRecord r;
     TileSpan sp{};
     const Viewport vp = to_vp(g);
@@ -87,14 +88,22 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
                              transform_vertex(mesh, M, i3), mesh.rgb + 3 * (size_t)t, g.w, g.h);
         sp = tile_span(vp, r);
         store_record(fb.records + tri_base + t, r, sp.ntiles);
-        large = sp.large;
+        direct = is_direct(r.x0, r.xe, r.y0, r.y1, g.direct_max);
+        large = sp.large && !direct;
     }
     // binning: count tiles of small triangles here, queue the rest for warps
-    count_small_tiles_warp(live && !large, r, vp, sp, bb.tile_count);
+    count_small_tiles_warp(live && !large && !direct, r, vp, sp, bb.tile_count);
     // warp-ballot compaction of the large-triangle queue
     if (__any_sync(0xffffffffu, large)) {
         const int q = large_slot(large, sp.ntiles, bb.large_count, bb.large_cap);
         if (q >= 0) bb.large_queue[q] = t;
+    }
+    // the smallest triangles fold their samples into the global keys here (direct.cuh)
+    if (__any_sync(0xffffffffu, direct)) {
+        const uint32_t frags = direct ? direct_raster(r, tri_base + t, g.w, g.pitch,
+                                                      reinterpret_cast<unsigned long long *>(fb.keys))
+                                      : 0u;
+        add_frags_warp(frags, fb.fragments);
     }
 }
 
@@ -152,11 +161,13 @@ cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
 // The resets of a frame (device error word, fragment counter, newline tree: frame) and of
 // a draw (tile entry counts, large-queue counters: draw) in one launch.
 __global__ void __launch_bounds__(256)
-frame_reset_kernel(FrameBuffers fb, BinBuffers bb, uint32_t nl_nodes, uint32_t ntiles, int frame, int draw)
+frame_reset_kernel(FrameBuffers fb, BinBuffers bb, uint32_t nl_nodes, uint32_t ntiles, int frame, int draw,
+                   int tiles_current)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (frame && i < nl_nodes) fb.nltree[i] = -1;
     if (draw && i < ntiles) bb.tile_count[i] = 0u;
+    if (tiles_current && i < ntiles) fb.tile_gen[i] = fb.gen;
     if (i == 0) {
         if (frame) {
             *fb.error = 0u;
@@ -167,10 +178,11 @@ frame_reset_kernel(FrameBuffers fb, BinBuffers bb, uint32_t nl_nodes, uint32_t n
 }
 
 cudaError_t launch_frame_reset(const FrameBuffers &fb, const BinBuffers &bb, uint32_t nl_nodes, uint32_t ntiles,
-                               bool frame, bool draw, cudaStream_t s)
+                               bool frame, bool draw, bool tiles_current, cudaStream_t s)
 {
-    const uint32_t n = max(frame ? nl_nodes : 1u, draw ? ntiles : 1u);
-    frame_reset_kernel<<<(n + 255) / 256, 256, 0, s>>>(fb, bb, nl_nodes, ntiles, frame ? 1 : 0, draw ? 1 : 0);
+    const uint32_t n = max(frame ? nl_nodes : 1u, (draw || tiles_current) ? ntiles : 1u);
+    frame_reset_kernel<<<(n + 255) / 256, 256, 0, s>>>(fb, bb, nl_nodes, ntiles, frame ? 1 : 0, draw ? 1 : 0,
+                                                       tiles_current ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -87,9 +87,11 @@ struct sloth_ctx {
     cudaEvent_t setup_ev = nullptr, nl_ev = nullptr;
     bool nl_pending = false;            // a newline fold not yet joined into the ctx stream
 
-    // instrumentation
+    // instrumentation and options
     int depth_cull = 1;
     int tile_shape = 0;
+    int direct_max = 0;            // SLOTH_OPTION_DIRECT_SAMPLES (applied at the next clear)
+    bool keys_current = false;     // every tile's keys cleared for the current generation
     bool timing = false;
     std::map<std::string, KernelClock> clocks;
     uint64_t launches = 0;
@@ -270,11 +272,18 @@ static sloth_status apply_resets(sloth_ctx *ctx, bool draw)
 {
     if (!ctx->reset_pending && !draw) return SLOTH_OK;
     const bool frame = ctx->reset_pending;
+    // a draw that folds small triangles straight into the global keys needs every tile's
+    // keys valid for this generation: cleared once per frame, the tiles made current
+    const bool tiles = draw && ctx->g.direct_max > 0 && !ctx->keys_current;
+    if (tiles)
+        CU(ctx, cudaMemsetAsync(ctx->fb.keys, 0xff,
+                                (size_t)ctx->g.pitch * ctx->g.nty * ctx->g.th * sizeof(uint64_t), ctx->stream));
     CU(ctx, timed(ctx, "reset", [&] {
            return launch_frame_reset(ctx->fb, ctx->bb, 2u * (uint32_t)ctx->g.nl_size,
-                                     (uint32_t)(ctx->g.ntx * ctx->g.nty), frame, draw, ctx->stream);
+                                     (uint32_t)(ctx->g.ntx * ctx->g.nty), frame, draw, tiles, ctx->stream);
        }));
     ctx->reset_pending = false;
+    if (tiles) ctx->keys_current = true;
     return SLOTH_OK;
 }
 
@@ -333,6 +342,7 @@ void sloth_ctx_unregister_batch(sloth_ctx *ctx, sloth_batch *b)
 int sloth_ctx_device(const sloth_ctx *ctx) { return ctx->device; }
 cudaStream_t sloth_ctx_stream(const sloth_ctx *ctx) { return ctx->stream; }
 int sloth_ctx_depth_cull(const sloth_ctx *ctx) { return ctx->depth_cull; }
+int sloth_ctx_direct_samples(const sloth_ctx *ctx) { return ctx->direct_max; }
 struct MeshView {
     const float *x, *y, *z;
     const uint32_t *idx;
@@ -576,6 +586,8 @@ sloth_status sloth_ctx_clear(sloth_ctx *ctx)
     }
     ctx->tri_base = 0;
     ctx->dirty = true;
+    ctx->g.direct_max = ctx->direct_max;
+    ctx->keys_current = false;
     return SLOTH_OK;
 }
 
@@ -915,6 +927,12 @@ sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value)
     case SLOTH_OPTION_DEPTH_CULL:
         if (value != 0 && value != 1) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "depth cull is 0 or 1");
         ctx->depth_cull = (int)value;
+        return SLOTH_OK;
+    case SLOTH_OPTION_DIRECT_SAMPLES:
+        if (value < 0 || value > SLOTH_MAX_DIRECT_SAMPLES)
+            return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "direct samples %lld outside 0..%d", (long long)value,
+                        SLOTH_MAX_DIRECT_SAMPLES);
+        ctx->direct_max = (int)value;
         return SLOTH_OK;
     default:
         return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "unknown option %d", option);

@@ -16,6 +16,10 @@ struct FrameGeom {
     int32_t w, h, image;
     int32_t tw, th, ntx, nty, pitch;
     int32_t nl_size;         // power of two >= h: leaves of the newline segment tree
+    int32_t direct_max;      // triangles whose sample range holds 1..direct_max samples are
+                             // rasterized by the setup kernel straight into the global keys
+                             // (direct.cuh) instead of being binned; 0: none.  Needs every
+                             // tile's keys valid for the current generation before setup.
 };
 
 // Device buffers of one frame (one Context).
@@ -95,9 +99,10 @@ struct Mat4 {
 int device_sm_count();
 
 // frame resets (error word, fragments, newline tree) and draw resets (tile counts, large
-// queue counters), either or both, in one launch.
+// queue counters), either or both, in one launch; tiles_current also sets every tile's
+// generation to the current one (its keys were cleared to the empty key before).
 cudaError_t launch_frame_reset(const FrameBuffers &fb, const BinBuffers &bb, uint32_t nl_nodes, uint32_t ntiles,
-                               bool frame, bool draw, cudaStream_t s);
+                               bool frame, bool draw, bool tiles_current, cudaStream_t s);
 
 // vertex transform: tv[i] = (M*v_i).xyz (nalgebra order), float4 per vertex.
 cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *tv,

@@ -24,6 +24,7 @@ ERR_INVALID_ARGUMENT, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_LIMIT, ERR_DEVICE_FAULT =
 OPTION_DEPTH_CULL = 1
 OPTION_TILE_SHAPE = 2
 OPTION_WAIT_TEST = 3
+OPTION_DIRECT_SAMPLES = 4
 STATUS ={0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "LIMIT", 5: "DEVICE_FAULT"}
 
 # Every symbol declared in include/sloth_gpu.h, with (restype, argtypes).
@@ -70,7 +71,8 @@ SIGNATURES = {
     "sloth_batch_frame_buffers": (C.c_int, [_vp, C.c_uint32, C.POINTER(_vp), C.POINTER(_vp)]),
     "sloth_batch_fragments": (C.c_int, [_vp, _u64p]),
     "sloth_batch_set_tile_shape": (C.c_int, [_vp, C.c_int]),
-    "sloth_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+    "sloth_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+    "sloth_batch_set_direct_samples": (C.c_int, [_vp, C.c_int]),
     "sloth_batch_depth_cells": (C.c_int, [_vp, C.c_uint32, _u64p, _u64p]),
     "sloth_ctx_flush": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_uint64, _u64p]),
     "sloth_ctx_read_async": (C.c_int, [_vp, _u32p, _f32p, _i32p]),
@@ -254,6 +256,11 @@ class Context:
         """SLOTH_OPTION_DEPTH_CULL: skip triangles proven hidden (same results)."""
         self._check(self.lib.sloth_ctx_set_option(self.h, OPTION_DEPTH_CULL, 1 if on else 0))
 
+    def set_direct_samples(self, samples: int):
+        """SLOTH_OPTION_DIRECT_SAMPLES: triangles of at most this many samples are folded
+        straight into the depth keys by setup (same results); applies at the next clear."""
+        self._check(self.lib.sloth_ctx_set_option(self.h, OPTION_DIRECT_SAMPLES, samples))
+
     def set_timing(self, on: bool):
         self._check(self.lib.sloth_ctx_set_timing(self.h, 1 if on else 0))
 
@@ -416,10 +423,14 @@ class Batch:
     def set_tile_shape(self, shape: int):
         self.ctx._check(self.lib.sloth_batch_set_tile_shape(self.h, shape))
 
+    def set_direct_samples(self, samples: int):
+        self.ctx._check(self.lib.sloth_batch_set_direct_samples(self.h, samples))
+
     def autotune(self, reps: int = 3):
-        s, ms = C.c_int(), C.c_float()
-        self.ctx._check(self.lib.sloth_batch_autotune(self.h, reps, C.byref(s), C.byref(ms)))
-        return s.value, ms.value
+        """(tile shape, direct-sample limit, mean render ms) of the fastest pair, now set."""
+        s, d, ms = C.c_int(), C.c_int(), C.c_float()
+        self.ctx._check(self.lib.sloth_batch_autotune(self.h, reps, C.byref(s), C.byref(d), C.byref(ms)))
+        return s.value, d.value, ms.value
 
     def flush(self, frame: int, fmt: int = 1) -> bytes:
         """Context::flush's stdout bytes for one frame, formatted on the GPU."""

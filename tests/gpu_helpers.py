@@ -6,8 +6,9 @@ import sloth_gpu as S
 from oracle import oracle as O
 
 
-def _render_once(ctx, dev_meshes, Rs, w, h, image, U, depth_cull):
+def _render_once(ctx, dev_meshes, Rs, w, h, image, U, depth_cull, direct=0):
     ctx.set_depth_cull(depth_cull)
+    ctx.set_direct_samples(direct)
     ctx.set_viewport(w, h, image)
     if U is None:
         ctx.update(dev_meshes)
@@ -23,9 +24,11 @@ def _render_once(ctx, dev_meshes, Rs, w, h, image, U, depth_cull):
 def gpu_render(ctx, meshes, R, w, h, image, U=None, dev_meshes=None, depth_cull=None):
     """Clear, draw every mesh in order, read back: (cells, z, winner, fragments).
 
-    depth_cull None renders twice, without depth culling (where every covered sample is
-    counted, so the fragment count is compared) and with it (buffers must be identical);
-    the returned tuple is the culled render with the unculled fragment count."""
+    depth_cull None renders four times: without depth culling (where every covered sample
+    is counted, so the fragment count is compared) and with it, each with every triangle
+    binned and with the small ones folded straight into the keys by setup (direct limits 64
+    and 16); all four buffers must be identical, and so must the two unculled fragment
+    counts.  The returned tuple is the culled, binned render with the unculled count."""
     if dev_meshes is None:
         dev_meshes = [S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"], m.get("idx"), m.get("bbox_max"))
                       for m in meshes]
@@ -35,12 +38,18 @@ def gpu_render(ctx, meshes, R, w, h, image, U=None, dev_meshes=None, depth_cull=
         return out if not depth_cull else (*out[:3], None)
     plain = _render_once(ctx, dev_meshes, Rs, w, h, image, U, False)
     culled = _render_once(ctx, dev_meshes, Rs, w, h, image, U, True)
-    for a, b, name in zip(plain[:3], culled[:3], ("cells", "z", "winner")):
-        assert np.array_equal(a.view(np.uint32) if a.dtype == np.float32 else a,
-                              b.view(np.uint32) if b.dtype == np.float32 else b), \
-            f"depth culling changed the {name} buffer"
-    assert culled[3] <= plain[3]
+    direct = _render_once(ctx, dev_meshes, Rs, w, h, image, U, False, direct=64)
+    direct_culled = _render_once(ctx, dev_meshes, Rs, w, h, image, U, True, direct=16)
+    for other, what in ((culled, "depth culling"), (direct, "the direct path"),
+                        (direct_culled, "the direct path with depth culling")):
+        for a, b, name in zip(plain[:3], other[:3], ("cells", "z", "winner")):
+            assert np.array_equal(a.view(np.uint32) if a.dtype == np.float32 else a,
+                                  b.view(np.uint32) if b.dtype == np.float32 else b), \
+                f"{what} changed the {name} buffer"
+    assert culled[3] <= plain[3] and direct_culled[3] <= plain[3]
+    assert direct[3] == plain[3], f"fragments: direct path {direct[3]}, binned {plain[3]}"
     ctx.set_depth_cull(True)
+    ctx.set_direct_samples(0)
     return (*culled[:3], plain[3])
 
 

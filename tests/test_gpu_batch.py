@@ -57,9 +57,11 @@ def check_frames(batch, meshes, frames, label):
         assert_same((cells, z, winner, None), ref, f"{label} frame {i} {f['w']}x{f['h']}")
 
 
-def test_batch_matches_oracle_and_replays(ctx):
+@pytest.mark.parametrize("direct", [0, 16])
+def test_batch_matches_oracle_and_replays(ctx, direct):
     meshes, dev, frames = mixed_frames(ctx)
     b = S.Batch(ctx, frames)
+    b.set_direct_samples(direct)
     b.render()                                   # planned render (sizes the entries)
     check_frames(b, meshes, frames, "planned")
     for k in range(3):                           # graph capture + replays
@@ -86,8 +88,12 @@ def test_batch_every_tile_shape_and_autotune(ctx):
         b.set_tile_shape(shape)
         b.render()
         check_frames(b, meshes, frames, f"shape {S.tile_shapes()[shape]}")
-    best, ms = b.autotune(reps=2)
-    assert 0 <= best < len(S.tile_shapes()) and ms > 0
+    for direct in (4, 64):
+        b.set_direct_samples(direct)
+        b.render()
+        check_frames(b, meshes, frames, f"direct {direct}")
+    best, direct, ms = b.autotune(reps=2)
+    assert 0 <= best < len(S.tile_shapes()) and direct in (0, 4, 16, 64) and ms > 0
     b.render()
     check_frames(b, meshes, frames, "autotuned")
     b.close()
@@ -128,7 +134,8 @@ def test_context_every_tile_shape(ctx, shape):
         ctx.set_tile_shape(0)
 
 
-def test_batch_dense_frames_split_tiles(ctx):
+@pytest.mark.parametrize("direct", [0, 64])
+def test_batch_dense_frames_split_tiles(ctx, direct):
     """Frames whose tiles hold more than 8192 entries (rasterized in slices) next to
     ordinary frames, planned and replayed."""
     dense = W.soup(50000, seed=43, n_large=3)
@@ -143,6 +150,7 @@ def test_batch_dense_frames_split_tiles(ctx):
         frames.append({"w": w, "h": h, "image": image, "U": U, "names": names, "R": R,
                        "draws": [(dev[n], R) for n in names]})
     b = S.Batch(ctx, frames)
+    b.set_direct_samples(direct)
     b.render()
     check_frames(b, meshes, frames, "planned")
     b.render()
