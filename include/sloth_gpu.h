@@ -213,7 +213,11 @@ sloth_status sloth_mesh_info(const sloth_mesh *mesh, uint32_t *ntri, float bbox_
 /* draw_mesh(context, mesh, transform, default_shader) (src/rasterizer.rs:39-46): draws
  * every triangle of `mesh` in order, after all triangles drawn since the last clear.
  * transform: the row-major rotation (or any model matrix); the library forms
- * utransform*transform once, in nalgebra's order.  Asynchronous on the ctx stream. */
+ * utransform*transform once, in nalgebra's order.  Asynchronous on the ctx stream: the
+ * host does not wait for the GPU, except on the context's first draw (which sizes the
+ * tile-entry buffer from its count) and when a buffer grows.  A draw whose tile entries
+ * outgrow the entry buffer is rasterized by a slower exact fallback on the device, and a
+ * later draw grows the buffer. */
 sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float transform[16]);
 
 /* ---- many frames at once --------------------------------------------------------- */

@@ -160,6 +160,7 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
         block_sync();
     }
     if (tid == 0) {
+        if (bb.max_total) atomicMax(bb.max_total, carry_e);
         bb.tile_offset[n] = carry_e;
         bb.slice_offset[n] = carry_h + carry_l;
         bb.slice_offset[n + 1] = sp.threshold;

@@ -74,6 +74,10 @@ struct sloth_ctx {
     size_t tv_cap = 0;
     uint32_t *h_total = nullptr;   // pinned
     cudaEvent_t total_ev = nullptr;   // h_total has arrived
+    uint32_t *d_max = nullptr;     // largest entry total of any draw (the scan's atomicMax)
+    uint32_t *h_max = nullptr;     // pinned copy of d_max
+    cudaEvent_t max_ev = nullptr;  // h_max has arrived
+    bool max_pending = false;      // a copy of d_max is on its way
     unsigned long long *h_frags = nullptr;   // pinned
     uint32_t *h_error = nullptr;   // pinned copy of fb.error
     uint32_t tri_base = 0;
@@ -467,7 +471,11 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
         cudaMallocHost(&ctx->h_frags, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMallocHost(&ctx->h_error, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->fb.error, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMemset(ctx->fb.error, 0, sizeof(uint32_t)) != cudaSuccess) {
+        cudaMemset(ctx->fb.error, 0, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_max, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_max, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemset(ctx->d_max, 0, sizeof(uint32_t)) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->max_ev, cudaEventDisableTiming) != cudaSuccess) {
         if (ctx->h_total) cudaFreeHost(ctx->h_total);
         if (ctx->total_ev) cudaEventDestroy(ctx->total_ev);
         if (ctx->scan_ev) cudaEventDestroy(ctx->scan_ev);
@@ -481,11 +489,16 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
         if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
         if (ctx->h_error) cudaFreeHost(ctx->h_error);
         if (ctx->fb.error) cudaFree(ctx->fb.error);
+        if (ctx->h_max) cudaFreeHost(ctx->h_max);
+        if (ctx->d_max) cudaFree(ctx->d_max);
+        if (ctx->max_ev) cudaEventDestroy(ctx->max_ev);
         if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         return SLOTH_ERR_OUT_OF_MEMORY;
     }
     *ctx->h_error = 0;
+    *ctx->h_max = 0;
+    ctx->bb.max_total = ctx->d_max;
     *out = ctx;
     return SLOTH_OK;
 }
@@ -525,6 +538,9 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     if (ctx->h_frags) cudaFreeHost(ctx->h_frags);
     if (ctx->h_error) cudaFreeHost(ctx->h_error);
     dfree(ctx->fb.error);
+    if (ctx->h_max) cudaFreeHost(ctx->h_max);
+    dfree(ctx->d_max);
+    if (ctx->max_ev) cudaEventDestroy(ctx->max_ev);
     flush_release(ctx->flush);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -824,6 +840,27 @@ sloth_status sloth_mesh_info(const sloth_mesh *m, uint32_t *ntri, float bbox_max
 // ---------------------------------------------------------------------------------------
 // draw_mesh
 // ---------------------------------------------------------------------------------------
+
+// Grows the tile-entry buffer once the device has reported (without the host waiting for
+// it) a draw whose entries exceeded it: such a draw was rasterized by the overflow
+// fallback, and the later ones get a buffer that fits.  The growth itself waits for the
+// context's stream (it frees the old buffer); it happens rarely, as the buffer doubles.
+static sloth_status poll_entry_max(sloth_ctx *ctx)
+{
+    if (!ctx->max_pending) return SLOTH_OK;
+    const cudaError_t q = cudaEventQuery(ctx->max_ev);
+    if (q == cudaErrorNotReady) return SLOTH_OK;
+    ctx->max_pending = false;
+    CU(ctx, q);
+    if (ctx->bb.entries && *ctx->h_max > ctx->bb.capacity) {
+        size_t ecap = ctx->bb.capacity;
+        sloth_status st = ensure_scratch(ctx, &ctx->bb.entries, &ecap, *ctx->h_max);
+        if (st != SLOTH_OK) return st;
+        ctx->bb.capacity = (uint32_t)(ecap > 0xffffffffu ? 0xffffffffu : ecap);
+    }
+    return SLOTH_OK;
+}
+
 sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float transform[16])
 {
     if (!ctx) return SLOTH_ERR_INVALID_ARGUMENT;
@@ -835,6 +872,7 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
         return fail(ctx, SLOTH_ERR_LIMIT, "more than %u triangles since the last clear", SLOTH_MAX_TRIANGLES);
     CU(ctx, cudaSetDevice(ctx->device));
     sloth_status st;
+    if ((st = poll_entry_max(ctx)) != SLOTH_OK) return st;
     if ((st = ensure_records(ctx, (size_t)ctx->tri_base + mesh->ntri)) != SLOTH_OK) return st;
     if (mesh->idx && (st = ensure_scratch(ctx, &ctx->tv, &ctx->tv_cap, mesh->nvert)) != SLOTH_OK) return st;
     if ((st = ensure_scratch(ctx, &ctx->bb.large_queue, &ctx->large_cap, mesh->ntri)) != SLOTH_OK) return st;
@@ -863,17 +901,13 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     ctx->nl_pending = true;
     CU(ctx, timed(ctx, "bin_count_large",[&] { return launch_bin_count_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
-    // the entry count comes back on a side stream, so that the draw's stream goes on
-    CU(ctx, cudaEventRecord(ctx->scan_ev, s));
-    CU(ctx, cudaStreamWaitEvent(ctx->side, ctx->scan_ev, 0));
-    CU(ctx, cudaMemcpyAsync(ctx->h_total, ctx->bb.tile_offset + ntiles, sizeof(uint32_t),
-                            cudaMemcpyDeviceToHost, ctx->side));
-    CU(ctx, cudaEventRecord(ctx->total_ev, ctx->side));
-    // The entry count sizes the entry buffer.  With a buffer from earlier draws the rest of
-    // the draw goes ahead with it while the host waits for the count: the fill kernels
-    // write no slot past the capacity and the raster does nothing when the count is above
-    // it.  Only then does the host grow the buffer and run the rest again, after a scan
-    // that resets the cursors.
+    // The entry count is known only on the device.  With an entry buffer from earlier draws
+    // the rest of the draw goes ahead with it and the host does not wait: the fill kernels
+    // write no slot past the capacity, the raster does nothing when the count is above it,
+    // and the overflow fallback then rasterizes the draw's binned triangles straight into
+    // the keys (the same keys).  The device's running maximum of the counts comes back on
+    // a side stream, and a later draw grows the buffer from it (poll_entry_max).  The first
+    // draw on a context, with no buffer yet, waits for its count and sizes the buffer.
     auto rest = [&](size_t entries_bound) -> sloth_status {
         // the small and the large fill take slots from the same cursors (atomics): they
         // run side by side, the large one on the aux stream
@@ -893,15 +927,29 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
         CU(ctx, timed(ctx, "raster", [&] { return launch_raster(g, ctx->fb, ctx->bb, ctx->depth_cull, s); }));
         return SLOTH_OK;
     };
-    const bool ahead = ctx->bb.entries && ctx->bb.capacity > 0;
-    if (ahead && (st = rest(ctx->bb.capacity)) != SLOTH_OK) return st;
-    CU(ctx, cudaEventSynchronize(ctx->total_ev));
-    const uint32_t total = *ctx->h_total;
-    if (!ahead || total > ctx->bb.capacity) {
+    if (ctx->bb.entries && ctx->bb.capacity > 0) {
+        if ((st = rest(ctx->bb.capacity)) != SLOTH_OK) return st;
+        CU(ctx, timed(ctx, "overflow", [&] {
+               return launch_overflow(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s);
+           }));
+        if (!ctx->max_pending) {
+            CU(ctx, cudaEventRecord(ctx->scan_ev, s));
+            CU(ctx, cudaStreamWaitEvent(ctx->side, ctx->scan_ev, 0));
+            CU(ctx, cudaMemcpyAsync(ctx->h_max, ctx->d_max, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->side));
+            CU(ctx, cudaEventRecord(ctx->max_ev, ctx->side));
+            ctx->max_pending = true;
+        }
+    } else {
+        CU(ctx, cudaEventRecord(ctx->scan_ev, s));
+        CU(ctx, cudaStreamWaitEvent(ctx->side, ctx->scan_ev, 0));
+        CU(ctx, cudaMemcpyAsync(ctx->h_total, ctx->bb.tile_offset + ntiles, sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost, ctx->side));
+        CU(ctx, cudaEventRecord(ctx->total_ev, ctx->side));
+        CU(ctx, cudaEventSynchronize(ctx->total_ev));
+        const uint32_t total = *ctx->h_total;
         size_t ecap = ctx->bb.capacity;
         if ((st = ensure_scratch(ctx, &ctx->bb.entries, &ecap, total)) != SLOTH_OK) return st;
         ctx->bb.capacity = (uint32_t)(ecap > 0xffffffffu ? 0xffffffffu : ecap);
-        if (ahead) CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
         if ((st = rest(total)) != SLOTH_OK) return st;
     }
     ctx->tri_base += mesh->ntri;

@@ -54,6 +54,7 @@ struct BinBuffers {
                              // slice size, [ntiles+3] = items of split tiles (listed first)
     uint2 *items;            // item_capacity: (tile, slice) of each raster CTA
     uint32_t item_capacity;
+    uint32_t *max_total;     // optional: the scan folds each draw's entry total in (atomicMax)
 };
 
 // A tile holding many more entries than the launch's mean is rasterized in slices by
@@ -130,6 +131,14 @@ cudaError_t launch_bin_fill_large(uint32_t tri_base, const FrameGeom &g, const F
 // per-tile raster: 64-bit atomicMin of depth keys in shared memory, merged into keys.
 cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb, int depth_cull,
                           cudaStream_t s);
+
+// A draw whose tile entries outgrew the entry buffer (the scan total is above the
+// capacity; its fill wrote what fitted and its raster did nothing) is rasterized here
+// instead: every tile not yet current gets empty keys, then one warp per binned triangle
+// folds its covered samples straight into the global keys.  Both kernels return at once
+// when the entries fitted.
+cudaError_t launch_overflow(uint32_t ntri, uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
+                            const BinBuffers &bb, cudaStream_t s);
 
 // resolve: keys -> z, frame cells, winners.
 cudaError_t launch_resolve(const FrameGeom &g, const FrameBuffers &fb, cudaStream_t s);

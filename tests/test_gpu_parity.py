@@ -241,6 +241,39 @@ def test_entry_buffer_grows_between_frames():
         c.close()
 
 
+@pytest.mark.parametrize("cull,direct", [(False, 0), (True, 0), (True, 16)])
+def test_overflow_fallback_multi_draw(cull, direct):
+    """Draws whose tile entries outgrow the entry buffer sized by a context's first frame:
+    the host does not wait for the count, so such a draw is rasterized by the device-side
+    fallback (every binned triangle folded straight into the keys), after the keys of the
+    frame's earlier draws and before those of its later draws."""
+    small = W.soup(100, seed=7)
+    big = W.soup(30000, seed=8, n_large=50)
+    big2 = W.soup(20000, seed=9, n_large=30, sigma=0.04)
+    R = O.euler_rotation(*W.cli_rotation(yaw=0.6))
+    c = S.Context(0)
+    try:
+        c.set_depth_cull(cull)
+        c.set_direct_samples(direct)
+        dev = [S.Mesh(c, m["x"], m["y"], m["z"], m["rgb"]) for m in (small, big, big2)]
+        c.set_viewport(320, 180, True)
+        c.update(dev[:1])
+        c.clear()
+        c.draw_mesh(dev[0], R)          # the first draw sizes the entry buffer: 100 triangles
+        c.read()
+        for w, h, image in ((640, 360, True), (641, 200, False)):
+            c.set_viewport(w, h, image)
+            c.update(dev)
+            c.clear()
+            for d in dev:
+                c.draw_mesh(d, R)
+            cells, z, winner = c.read()
+            ref = oracle_render([small, big, big2], R, w, h, image)
+            assert_same((cells, z, winner, None if cull else c.fragments()), ref, f"overflow {w}x{h}")
+    finally:
+        c.close()
+
+
 def test_many_frames_generation_counter(ctx):
     """Repeated clears reuse the key buffer through the tile generation counter."""
     m = W.soup(300, seed=1)
