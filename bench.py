@@ -574,12 +574,22 @@ def run_config3(torch, stream, device, args):
     torch.cuda.synchronize()
     steps = max(3, args.batched_steps)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    for _ in range(steps):
+
+    def time_batched():
         batch.render()
-    b.record(stream)
-    torch.cuda.synchronize()
-    batched_ms = a.elapsed_time(b) / steps
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(steps):
+            batch.render()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps
+
+    # the raster as one CTA per item, for comparison with the persistent queue
+    batch.set_persistent(False)
+    per_item_ms = time_batched()
+    batch.set_persistent(True)
+    batched_ms = time_batched()
 
     plain = {}
     def plain_pass():
@@ -615,7 +625,8 @@ def run_config3(torch, stream, device, args):
            "batched_frames_per_s": 1000.0 * nframes / batched_ms, "batched_ms_per_pass": batched_ms,
            "plain_frames_per_s": 1000.0 * nframes / plain_ms, "plain_ms_per_pass": plain_ms,
            "batched_over_plain": plain_ms / batched_ms, "tile_shape": S.tile_shapes()[shape],
-           "direct_samples": direct, "graph": True}
+           "direct_samples": direct, "raster": "persistent: SMs x resident CTAs over the device item queue",
+           "one_cta_per_item_ms_per_pass": per_item_ms, "graph": True}
     if par is not None:
         out["bitexact_frames_vs_oracle"] = par["frames_bitexact"]
         out["parity_vs_oracle"] = par

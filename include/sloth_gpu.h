@@ -267,6 +267,10 @@ sloth_status sloth_batch_flush(sloth_batch *batch, uint32_t frame, int format, c
                                uint64_t *bytes);
 /* Use tile shape `shape` (sloth_tile_shape) for this batch; re-lays out its buffers. */
 sloth_status sloth_batch_set_tile_shape(sloth_batch *batch, int shape);
+/* persistent != 0 (the default): the raster is a grid of SMs x resident CTAs that take
+ * (frame, tile) items from a device-side queue until it is empty; 0: one CTA per item,
+ * balanced by the hardware block scheduler.  The frames are the same either way. */
+sloth_status sloth_batch_set_persistent(sloth_batch *batch, int persistent);
 /* Rasterize triangles of at most `samples` samples straight into the depth keys during
  * setup (SLOTH_OPTION_DIRECT_SAMPLES for a batch; a new batch takes its context's value). */
 sloth_status sloth_batch_set_direct_samples(sloth_batch *batch, int samples);

@@ -184,6 +184,7 @@ __device__ __forceinline__ uint32_t frame_of_tile(const BatchDev &b, uint32_t ti
 __global__ void __launch_bounds__(256) batch_items_kernel(BatchDev b)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) *b.queue = 0u;   // the persistent raster's item counter
     if (t >= b.total_tiles) return;
     const uint32_t nt = b.total_tiles;
     const SplitParams sp{b.bb.slice_offset[nt + 1], b.bb.slice_offset[nt + 2]};
@@ -205,27 +206,52 @@ __global__ void __launch_bounds__(256) batch_items_kernel(BatchDev b)
     }
 }
 
-// Raster over every frame's tiles in one launch: CTA i rasterizes raster item i (a tile,
-// or a slice of a split tile) of the item list built by batch_items_kernel; the hardware
-// block scheduler keeps the SMs fed as CTAs finish.  CTAs past the item count return.
+// Raster item i (a tile, or a slice of a split tile, of any frame) of the item list built by
+// batch_items_kernel; false when its key load gave up (raster_tile).
 template <int TW, int TH>
-__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) batch_raster_kernel(BatchDev b)
+__device__ __forceinline__ bool batch_raster_item(TileSmem<TW, TH> &S, const BatchDev &b, uint32_t i, uint32_t &phase)
 {
-    __shared__ TileSmem<TW, TH> S;
-    if (b.bb.tile_offset[b.total_tiles] > b.bb.capacity) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) *b.overflow = 1;
-        return;
-    }
-    if (blockIdx.x >= b.bb.slice_offset[b.total_tiles] || blockIdx.x >= b.bb.item_capacity) return;
-    const uint2 it = b.bb.items[blockIdx.x];
+    const uint2 it = b.bb.items[i];
     const BatchFrame &f = b.frames[frame_of_tile(b, it.x)];
     const uint32_t all = b.bb.tile_count[it.x];
     const uint32_t thr = b.bb.slice_offset[b.total_tiles + 1], slice = b.bb.slice_offset[b.total_tiles + 2];
     const bool split = all > thr;
     const uint32_t first = split ? it.y * slice : 0u;
     const uint32_t cnt = split ? min(slice, all - first) : all;
-    raster_tile<TW, TH>(S, f.g, f.fb, (int)(it.x - f.tile_off), cnt, b.bb.entries + b.bb.tile_offset[it.x] + first,
-                        b.depth_cull, split);
+    return raster_tile<TW, TH>(S, f.g, f.fb, (int)(it.x - f.tile_off), cnt,
+                               b.bb.entries + b.bb.tile_offset[it.x] + first, b.depth_cull, phase, split);
+}
+
+// Raster over every frame's tiles in one launch.  Persistent form (the default): a grid of
+// SMs x resident CTAs, each CTA taking the next item of the device-side (frame, tile)
+// queue -- the item list, split tiles' slices first -- from a counter (b.queue, zeroed by
+// batch_items_kernel) until the queue is empty.  The item is claimed by thread 0 and read
+// by every thread after a barrier, so the whole CTA leaves the loop together.  The other
+// form launches one CTA per item and leaves the balancing to the hardware block scheduler.
+template <int TW, int TH, bool kPersistent>
+__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) batch_raster_kernel(BatchDev b)
+{
+    __shared__ TileSmem<TW, TH> S;
+    __shared__ uint32_t s_item;
+    if (b.bb.tile_offset[b.total_tiles] > b.bb.capacity) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *b.overflow = 1;
+        return;
+    }
+    const uint32_t nitems = min(b.bb.slice_offset[b.total_tiles], b.bb.item_capacity);
+    if (!kPersistent && blockIdx.x >= nitems) return;
+    raster_barrier_init(S);
+    uint32_t phase = 0;
+    if (!kPersistent) {
+        batch_raster_item<TW, TH>(S, b, blockIdx.x, phase);
+        return;
+    }
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(b.queue, 1u);
+        block_sync();
+        const uint32_t i = s_item;   // thread 0 writes the next claim only after raster_tile's last barrier
+        if (i >= nitems) break;
+        if (!batch_raster_item<TW, TH>(S, b, i, phase)) break;
+    }
 }
 
 // blocks[i] = (frame, first cell).
@@ -288,14 +314,33 @@ cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nb
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, cudaStream_t s)
+// Resident CTAs per SM of a raster kernel (looked up once per kernel and device).
+template <class K>
+static int resident_ctas(K kernel)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kRasterThreads, 0) != cudaSuccess || n < 1) n = 1;
+    return n;
+}
+
+cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, bool persistent, cudaStream_t s)
 {
     if (!b.total_tiles) return cudaSuccess;
-    // one CTA per possible raster item; CTAs past the item count exit at once
-    const uint32_t grid = b.bb.item_capacity;
+    // persistent: SMs x resident CTAs take items from the queue; otherwise one CTA per
+    // possible raster item, CTAs past the item count exiting at once
 #define SLOTH_BATCH_RASTER_CASE(W_, H_)                                                        \
     if (tw == W_ && th == H_) {                                                                \
-        batch_raster_kernel<W_, H_><<<grid, kRasterThreads, 0, s>>>(b);                        \
+        if (persistent) {                                                                      \
+            static int per_sm[64];                                                             \
+            int dev = 0;                                                                       \
+            cudaGetDevice(&dev);                                                               \
+            if (dev >= 0 && dev < 64 && !per_sm[dev]) per_sm[dev] = resident_ctas(batch_raster_kernel<W_, H_, true>); \
+            const uint32_t slots = (uint32_t)device_sm_count() * (dev >= 0 && dev < 64 ? per_sm[dev] : 1); \
+            const uint32_t grid = slots < b.bb.item_capacity ? slots : b.bb.item_capacity;     \
+            batch_raster_kernel<W_, H_, true><<<grid, kRasterThreads, 0, s>>>(b);              \
+        } else {                                                                               \
+            batch_raster_kernel<W_, H_, false><<<b.bb.item_capacity, kRasterThreads, 0, s>>>(b); \
+        }                                                                                      \
         return cudaGetLastError();                                                             \
     }
     SLOTH_TILE_SHAPES(SLOTH_BATCH_RASTER_CASE)

@@ -34,6 +34,7 @@ struct sloth_batch {
     std::vector<float> transforms;            // 16 per draw
     int shape = 0;
     int direct_max = 0;                       // FrameGeom::direct_max of every frame
+    bool persistent = true;                   // raster over the device queue (else one CTA per item)
 
     // layout (per shape)
     std::vector<BatchFrame> hframes;
@@ -61,6 +62,7 @@ struct sloth_batch {
     size_t entries_cap = 0;
     uint32_t *large_frame = nullptr;
     uint32_t *overflow = nullptr;
+    uint32_t *queue = nullptr;                // the persistent raster's item counter
     uint32_t *h_total = nullptr;              // pinned
     uint32_t *h_overflow = nullptr;           // pinned
     uint32_t *error = nullptr;                // device error word of the raster (sticky)
@@ -155,6 +157,7 @@ void free_layout(sloth_batch *b)
     bfree(b->bb.items);
     b->bb.item_capacity = 0;
     bfree(b->overflow);
+    bfree(b->queue);
     for (auto &p : b->blk) bfree(p);
     b->entries_cap = 0;
     b->rendered = false;
@@ -275,6 +278,7 @@ sloth_status build(sloth_batch *b, int shape)
     BCU(b, balloc(&b->large_frame, rec));
     BCU(b, balloc(&b->bb.slice_offset, tiles + 4));
     BCU(b, balloc(&b->overflow, 1));
+    BCU(b, balloc(&b->queue, 1));
     BCU(b, balloc(&b->d_mats, nd));
     for (uint32_t f = 0; f < nf; ++f) {
         BatchFrame &bf = b->hframes[f];
@@ -319,6 +323,7 @@ BatchDev dev_view(sloth_batch *b)
     d.bb.capacity = (uint32_t)(b->entries_cap > 0xffffffffu ? 0xffffffffu : b->entries_cap);
     d.large_frame = b->large_frame;
     d.overflow = b->overflow;
+    d.queue = b->queue;
     d.depth_cull = sloth_ctx_depth_cull(b->ctx);
     return d;
 }
@@ -364,7 +369,7 @@ cudaError_t enqueue_back(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     if ((e = cudaStreamWaitEvent(s, b->ev_aux, 0))) return e;
     if ((e = launch_batch_items(d, s))) return e;
     const int tw = kTileShapes[b->shape][0], th = kTileShapes[b->shape][1];
-    if ((e = launch_batch_raster(d, tw, th, s))) return e;
+    if ((e = launch_batch_raster(d, tw, th, b->persistent, s))) return e;
     if ((e = cudaStreamWaitEvent(s, b->ev_nl, 0))) return e;   // the newline tree is complete
     return launch_batch_resolve(d, b->blk[3], b->nblk[3], s);
 }
@@ -656,6 +661,20 @@ sloth_status sloth_batch_set_tile_shape(sloth_batch *b, int shape)
     BCU(b, cudaSetDevice(b->device));
     BCU(b, cudaStreamSynchronize(b->stream));
     return shape == b->shape ? SLOTH_OK : build(b, shape);
+}
+
+sloth_status sloth_batch_set_persistent(sloth_batch *b, int persistent)
+{
+    if (!b || !b->ctx) return SLOTH_ERR_INVALID_ARGUMENT;
+    BCU(b, cudaSetDevice(b->device));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    if ((persistent != 0) == b->persistent) return SLOTH_OK;
+    b->persistent = persistent != 0;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);   // the raster launch is part of the graph
+        b->graph = nullptr;
+    }
+    return SLOTH_OK;
 }
 
 sloth_status sloth_batch_set_direct_samples(sloth_batch *b, int samples)

@@ -43,6 +43,7 @@ struct BatchDev {
     BinBuffers bb;             // global tile arrays and entries
     uint32_t *large_frame;     // frame of each large-queue entry
     uint32_t *overflow;        // set when the entries outgrew their capacity
+    uint32_t *queue;           // the persistent raster's next item (zeroed by the item kernel)
     int depth_cull;
 };
 
@@ -54,7 +55,7 @@ cudaError_t launch_batch_newline(const BatchDev &b, const int2 *blocks, uint32_t
 cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s);
 cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s);
 cudaError_t launch_batch_items(const BatchDev &b, cudaStream_t s);
-cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, cudaStream_t s);
+cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, bool persistent, cudaStream_t s);
 cudaError_t launch_batch_resolve(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s);
 cudaError_t prepare_batch_kernels();
 

@@ -12,14 +12,17 @@ raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb, uint32_t ntiles, int 
 {
     __shared__ TileSmem<TW, TH> S;
     if (blockIdx.x >= bb.slice_offset[ntiles] || blockIdx.x >= bb.item_capacity) return;
-    if (bb.tile_offset[ntiles] > bb.capacity) return;   // entries past the buffer: the host runs it again
+    if (bb.tile_offset[ntiles] > bb.capacity) return;   // entries past the buffer: launch_overflow does it
     const uint2 it = bb.items[blockIdx.x];
     const uint32_t all = bb.tile_count[it.x];
     const uint32_t thr = bb.slice_offset[ntiles + 1], slice = bb.slice_offset[ntiles + 2];
     const bool split = all > thr;
     const uint32_t first = split ? it.y * slice : 0u;
     const uint32_t cnt = split ? min(slice, all - first) : all;
-    raster_tile<TW, TH>(S, g, fb, (int)it.x, cnt, bb.entries + bb.tile_offset[it.x] + first, depth_cull, split);
+    raster_barrier_init(S);
+    uint32_t phase = 0;
+    raster_tile<TW, TH>(S, g, fb, (int)it.x, cnt, bb.entries + bb.tile_offset[it.x] + first, depth_cull, phase,
+                        split);
 }
 
 // Overflow fallback, step 1: grid-stride over tiles, one warp per tile; a tile whose keys

@@ -327,14 +327,28 @@ __device__ __forceinline__ void refresh_bounds(TileSmem<TW, TH> &S, int R0, int 
     }
 }
 
-// Rasterize one tile of one frame: `cnt` entries at `entries`.  Called by all threads of
-// the CTA; returns after the tile's keys are stored and its generation is set.  A slice
-// of a split tile (split true) starts from empty keys and folds its keys into the tile's
-// with a global atomicMin; the tile's keys and generation were prepared before the launch.
+// The tile-load barrier, initialised once per CTA before its first raster_tile (called by
+// all threads).  raster_tile keeps its phase parity in `phase` (0 after the init).
 template <int TW, int TH>
-__device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom &g, const FrameBuffers &fb,
+__device__ __forceinline__ void raster_barrier_init(TileSmem<TW, TH> &S)
+{
+    if (threadIdx.x == 0) {
+        mbar_init(&S.kbar, 1);
+        fence_proxy_async_smem();
+    }
+    block_sync();
+}
+
+// Rasterize one tile of one frame: `cnt` entries at `entries`.  Called by all threads of
+// the CTA; returns after the tile's keys are stored and its generation is set, true, or
+// false when the load of an earlier draw's keys did not arrive (the tile is left as it
+// is, the error word is set, and the CTA must take no further tile).  A slice of a split
+// tile (split true) starts from empty keys and folds its keys into the tile's with a
+// global atomicMin; the tile's keys and generation were prepared before the launch.
+template <int TW, int TH>
+__device__ __forceinline__ bool raster_tile(TileSmem<TW, TH> &S, const FrameGeom &g, const FrameBuffers &fb,
                                             int tile, uint32_t cnt, const uint64_t *__restrict__ entries,
-                                            int depth_cull, bool split = false)
+                                            int depth_cull, uint32_t &phase, bool split = false)
 {
     static_assert(TH <= 32, "a tile part has at most 32 rows: one lane per row in raster_part");
     const int tr = tile / g.ntx, tc = tile - (tile / g.ntx) * g.ntx;
@@ -345,12 +359,9 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         // keys of earlier draws since the clear: one bulk copy per tile row (TW*8 bytes,
         // 16-byte aligned at both ends), completing on an mbarrier
         if (threadIdx.x < 32) {
-            // warp 0: lane 0 arms the barrier, then the lanes issue one row each
-            if (threadIdx.x == 0) {
-                mbar_init(&S.kbar, 1);
-                fence_proxy_async_smem();
+            // warp 0: lane 0 arms the barrier for this phase, then the lanes issue one row each
+            if (threadIdx.x == 0)
                 mbar_expect_tx(&S.kbar, (uint32_t)(TH * TW * sizeof(unsigned long long)) + (fb.wait_test ? 16u : 0u));
-            }
             __syncwarp();
             for (int rr = threadIdx.x; rr < TH; rr += 32)
                 bulk_load(&S.keys[rr * TW], gk + (size_t)rr * g.pitch, TW * sizeof(unsigned long long), &S.kbar);
@@ -358,13 +369,14 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         block_sync();
         if (threadIdx.x == 0) {
             const uint32_t polls = fb.wait_test ? kTestWaitPolls : kWaitPolls;
-            S.kok = (mbar_wait(&S.kbar, 0, polls) || mbar_wait(&S.kbar, 0, polls)) ? 1u : 0u;
+            S.kok = (mbar_wait(&S.kbar, phase, polls) || mbar_wait(&S.kbar, phase, polls)) ? 1u : 0u;
         }
         block_sync();
+        phase ^= 1u;
         if (!S.kok) {
             // the copy did not arrive: report it and leave the tile as it is
             if (threadIdx.x == 0 && fb.error) atomicOr(fb.error, 1u);
-            return;
+            return false;
         }
     } else {
         for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) S.keys[i] = kEmptyKey;
@@ -576,6 +588,7 @@ __device__ __forceinline__ void raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         __syncwarp();
     }
     block_sync();
+    return true;
 }
 
 }  // namespace sloth

@@ -73,6 +73,7 @@ SIGNATURES = {
     "sloth_batch_set_tile_shape": (C.c_int, [_vp, C.c_int]),
     "sloth_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "sloth_batch_set_direct_samples": (C.c_int, [_vp, C.c_int]),
+    "sloth_batch_set_persistent": (C.c_int, [_vp, C.c_int]),
     "sloth_batch_depth_cells": (C.c_int, [_vp, C.c_uint32, _u64p, _u64p]),
     "sloth_ctx_flush": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_uint64, _u64p]),
     "sloth_ctx_read_async": (C.c_int, [_vp, _u32p, _f32p, _i32p]),
@@ -425,6 +426,10 @@ class Batch:
 
     def set_direct_samples(self, samples: int):
         self.ctx._check(self.lib.sloth_batch_set_direct_samples(self.h, samples))
+
+    def set_persistent(self, on: bool):
+        """Persistent raster over the device-side item queue (default) or one CTA per item."""
+        self.ctx._check(self.lib.sloth_batch_set_persistent(self.h, 1 if on else 0))
 
     def autotune(self, reps: int = 3):
         """(tile shape, direct-sample limit, mean render ms) of the fastest pair, now set."""

@@ -57,11 +57,12 @@ def check_frames(batch, meshes, frames, label):
         assert_same((cells, z, winner, None), ref, f"{label} frame {i} {f['w']}x{f['h']}")
 
 
-@pytest.mark.parametrize("direct", [0, 16])
-def test_batch_matches_oracle_and_replays(ctx, direct):
+@pytest.mark.parametrize("direct,persistent", [(0, True), (16, True), (0, False)])
+def test_batch_matches_oracle_and_replays(ctx, direct, persistent):
     meshes, dev, frames = mixed_frames(ctx)
     b = S.Batch(ctx, frames)
     b.set_direct_samples(direct)
+    b.set_persistent(persistent)
     b.render()                                   # planned render (sizes the entries)
     check_frames(b, meshes, frames, "planned")
     for k in range(3):                           # graph capture + replays
@@ -134,8 +135,8 @@ def test_context_every_tile_shape(ctx, shape):
         ctx.set_tile_shape(0)
 
 
-@pytest.mark.parametrize("direct", [0, 64])
-def test_batch_dense_frames_split_tiles(ctx, direct):
+@pytest.mark.parametrize("direct,persistent", [(0, True), (64, True), (0, False)])
+def test_batch_dense_frames_split_tiles(ctx, direct, persistent):
     """Frames whose tiles hold more than 8192 entries (rasterized in slices) next to
     ordinary frames, planned and replayed."""
     dense = W.soup(50000, seed=43, n_large=3)
@@ -151,6 +152,7 @@ def test_batch_dense_frames_split_tiles(ctx, direct):
                        "draws": [(dev[n], R) for n in names]})
     b = S.Batch(ctx, frames)
     b.set_direct_samples(direct)
+    b.set_persistent(persistent)
     b.render()
     check_frames(b, meshes, frames, "planned")
     b.render()
