@@ -298,6 +298,7 @@ def run_gpu(args):
     R = S.euler_rotation(*W.cli_rotation())
 
     ctx = S.Context(local, stream=stream.cuda_stream)
+    ctx.set_direct_samples(args.direct)
     dm = S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"])
     ctx.set_viewport(W_PX, H_PX, True)
     ctx.update([dm])
@@ -398,6 +399,7 @@ def run_gpu(args):
         extra = []
         for _ in range(args.e2e_contexts - 1):
             c2 = S.Context(local)
+            c2.set_direct_samples(args.direct)
             c2.set_viewport(W_PX, H_PX, True)
             d2 = S.Mesh(c2, m["x"], m["y"], m["z"], m["rgb"])
             c2.update([d2])
@@ -512,7 +514,7 @@ def run_gpu(args):
                    "l2": "flushed before every timed step (512 MiB write)", "parallelism": f"replicas x{ws}"},
         "gfrag_per_s": frags * value / 1e9, "fragments_per_frame": frags,
         "fragments_rasterized_per_frame": frags_evaluated,
-        "depth_cull": not args.no_depth_cull,
+        "depth_cull": not args.no_depth_cull, "direct_samples": args.direct,
         "e2e": e2e,
         "gpu_launches": launches, "kernels": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
         "batched": batched, "differentiable": differentiable, "inverse_rendering": inverse,
@@ -597,7 +599,10 @@ def run_config3(torch, stream, device, args):
             key = (f["w"], f["h"], f["image"])
             c = plain.get(key)
             if c is None:
+                # the same kernels and settings as the batch: only the launch structure differs
                 c = plain[key] = S.Context(device, stream=stream.cuda_stream)
+                c.set_tile_shape(shape)
+                c.set_direct_samples(direct)
                 c.set_viewport(f["w"], f["h"], f["image"])
             c.set_utransform(f["U"])
             c.clear()
@@ -830,6 +835,8 @@ def main():
                     help="also time one whole config-2 frame on one thread (about a minute) beside the sample")
     ap.add_argument("--no-depth-cull", action="store_true",
                     help="rasterize every triangle (SLOTH_OPTION_DEPTH_CULL 0)")
+    ap.add_argument("--direct", type=int, default=0,
+                    help="SLOTH_OPTION_DIRECT_SAMPLES of the config-2 contexts (0: every triangle binned)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the full-size checks against the oracle (config 2 frame, every config-3 frame)")
