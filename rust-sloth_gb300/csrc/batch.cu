@@ -254,18 +254,22 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) batch_raster
     }
 }
 
-// blocks[i] = (frame, first cell).
+// blocks[i] = (frame, first cell): runs of 4 frame cells per lane (resolve_run), written
+// with one 16-byte store per buffer when the frame's outputs are aligned.
+constexpr int kBatchRun = 4;
+static_assert(kBatchResolveChunk % (kBatchRun * 256) == 0, "whole runs, the same trip count in every warp");
+
 __global__ void __launch_bounds__(256) batch_resolve_kernel(BatchDev b, const int2 *__restrict__ blocks)
 {
     const int2 blk = blocks[blockIdx.x];
     const BatchFrame &f = b.frames[blk.x];
     const uint64_t nz = (uint64_t)f.g.w * f.g.h;
     const uint64_t ncells = f.g.image ? nz + f.g.h : nz;
-    const uint64_t end = min(ncells, (uint64_t)blk.y + kBatchResolveChunk);   // chunks start even
+    const uint64_t end = min(ncells, (uint64_t)blk.y + kBatchResolveChunk);   // chunks start on runs
     const int lane = threadIdx.x & 31;
-    for (uint32_t i = threadIdx.x; i < kBatchResolveChunk / 2; i += blockDim.x) {
-        const uint64_t p = (uint64_t)blk.y / 2 + i;
-        resolve_pair(f.g, f.fb, p, 2 * p < end, lane);
+    for (uint32_t i = threadIdx.x; i < kBatchResolveChunk / kBatchRun; i += blockDim.x) {
+        const uint64_t p = (uint64_t)blk.y / kBatchRun + i;
+        resolve_run<kBatchRun>(f.g, f.fb, p, kBatchRun * p < end, lane, f.vec != 0);
     }
 }
 
