@@ -567,11 +567,14 @@ def run_config3(torch, stream, device, args):
     batch = S.Batch(ctx, frames)
     batch.render()
     if args.batched_shape >= 0:
-        shape, direct = args.batched_shape, max(0, args.batched_direct)
-        batch.set_tile_shape(shape)
-        batch.set_direct_samples(direct)
+        tuned = {"shape": args.batched_shape, "direct": max(0, args.batched_direct), "tpb": args.batched_tpb,
+                 "persistent": True}
+        batch.set_tile_shape(tuned["shape"])
+        batch.set_direct_samples(tuned["direct"])
+        batch.set_triangles_per_block(tuned["tpb"])
     else:
-        shape, direct, _ = batch.autotune(reps=2)
+        tuned = batch.autotune(reps=2)
+    shape, direct, tpb = tuned["shape"], tuned["direct"], tuned["tpb"]
     batch.render()
     torch.cuda.synchronize()
     steps = max(3, args.batched_steps)
@@ -587,11 +590,12 @@ def run_config3(torch, stream, device, args):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / steps
 
-    # the raster as one CTA per item, for comparison with the persistent queue
-    batch.set_persistent(False)
-    per_item_ms = time_batched()
-    batch.set_persistent(True)
-    batched_ms = time_batched()
+    # the raster as one CTA per item and over the persistent queue (the tuned form last)
+    forms = {}
+    for persistent in (not tuned["persistent"], tuned["persistent"]):
+        batch.set_persistent(persistent)
+        forms[persistent] = time_batched()
+    batched_ms = forms[tuned["persistent"]]
 
     plain = {}
     def plain_pass():
@@ -603,6 +607,7 @@ def run_config3(torch, stream, device, args):
                 c = plain[key] = S.Context(device, stream=stream.cuda_stream)
                 c.set_tile_shape(shape)
                 c.set_direct_samples(direct)
+                c.set_triangles_per_block(tpb)
                 c.set_viewport(f["w"], f["h"], f["image"])
             c.set_utransform(f["U"])
             c.clear()
@@ -630,8 +635,11 @@ def run_config3(torch, stream, device, args):
            "batched_frames_per_s": 1000.0 * nframes / batched_ms, "batched_ms_per_pass": batched_ms,
            "plain_frames_per_s": 1000.0 * nframes / plain_ms, "plain_ms_per_pass": plain_ms,
            "batched_over_plain": plain_ms / batched_ms, "tile_shape": S.tile_shapes()[shape],
-           "direct_samples": direct, "raster": "persistent: SMs x resident CTAs over the device item queue",
-           "one_cta_per_item_ms_per_pass": per_item_ms, "graph": True}
+           "direct_samples": direct, "triangles_per_block": tpb,
+           "raster": ("persistent: SMs x resident CTAs over the device item queue" if tuned["persistent"]
+                      else "one CTA per item"),
+           "persistent_ms_per_pass": forms[True], "one_cta_per_item_ms_per_pass": forms[False],
+           "autotuned": args.batched_shape < 0, "graph": True}
     if par is not None:
         out["bitexact_frames_vs_oracle"] = par["frames_bitexact"]
         out["parity_vs_oracle"] = par
@@ -849,6 +857,8 @@ def main():
                     help="tile shape of the config-3 batch (default: autotuned with the direct limit)")
     ap.add_argument("--batched-direct", type=int, default=0,
                     help="direct-sample limit of the config-3 batch when --batched-shape fixes the shape")
+    ap.add_argument("--batched-tpb", type=int, default=256,
+                    help="triangles per setup/fill block of the config-3 batch when --batched-shape fixes the shape")
     ap.add_argument("--only-diff", action="store_true", help="run only the differentiable legs (configs 4 and 5)")
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     args = ap.parse_args()

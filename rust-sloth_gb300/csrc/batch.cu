@@ -49,8 +49,9 @@ __global__ void __launch_bounds__(256) batch_vertex_kernel(BatchDev b, const int
                                      row_dot(&M.m[8], xs[k], ys[k], zs[k]), 0.0f);
 }
 
-// blocks[i] = (draw, first triangle): records, small-triangle tile counts, large queue.
-__global__ void __launch_bounds__(kBatchSetupBlock) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
+// blocks[i] = (draw, first triangle; b.tpb triangles): records, small-triangle tile
+// counts, large queue, and the direct folds of the smallest triangles.
+__global__ void __launch_bounds__(kMaxTrianglesPerBlock) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
 {
     const int2 blk = blocks[blockIdx.x];
     const BatchDraw &d = b.draws[blk.x];
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(256) batch_bin_large_kernel(BatchDev b)
 }
 
 // blocks[i] = (draw, first triangle): small triangles' tile entries.
-__global__ void __launch_bounds__(kBatchSetupBlock) batch_fill_kernel(BatchDev b, const int2 *__restrict__ blocks)
+__global__ void __launch_bounds__(kMaxTrianglesPerBlock) batch_fill_kernel(BatchDev b, const int2 *__restrict__ blocks)
 {
     const int2 blk = blocks[blockIdx.x];
     const BatchDraw &d = b.draws[blk.x];
@@ -289,7 +290,8 @@ cudaError_t launch_batch_vertex(const BatchDev &b, const int2 *blocks, uint32_t 
 cudaError_t launch_batch_setup(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s)
 {
     if (!nblocks) return cudaSuccess;
-    batch_setup_kernel<<<nblocks, kBatchSetupBlock, 0, s>>>(b, blocks);
+    if (!valid_triangles_per_block(b.tpb)) return cudaErrorInvalidValue;
+    batch_setup_kernel<<<nblocks, b.tpb, 0, s>>>(b, blocks);
     return cudaGetLastError();
 }
 
@@ -314,7 +316,8 @@ cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s)
 cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s)
 {
     if (!nblocks) return cudaSuccess;
-    batch_fill_kernel<<<nblocks, kBatchSetupBlock, 0, s>>>(b, blocks);
+    if (!valid_triangles_per_block(b.tpb)) return cudaErrorInvalidValue;
+    batch_fill_kernel<<<nblocks, b.tpb, 0, s>>>(b, blocks);
     return cudaGetLastError();
 }
 

@@ -35,6 +35,7 @@ struct sloth_batch {
     int shape = 0;
     int direct_max = 0;                       // FrameGeom::direct_max of every frame
     bool persistent = true;                   // raster over the device queue (else one CTA per item)
+    int tpb = kDefaultTrianglesPerBlock;      // triangles per setup/fill block
 
     // layout (per shape)
     std::vector<BatchFrame> hframes;
@@ -237,7 +238,7 @@ sloth_status build(sloth_batch *b, int shape)
             bd.local_base = local;
             bd.vert_off = (uint32_t)vert;
             for (uint32_t q = 0; q < (mv.nvert + 3) / 4; q += 256) bv.push_back(make_int2((int)d, (int)q));
-            for (uint32_t t = 0; t < mv.ntri; t += kBatchSetupBlock) bt.push_back(make_int2((int)d, (int)t));
+            for (uint32_t t = 0; t < mv.ntri; t += (uint32_t)b->tpb) bt.push_back(make_int2((int)d, (int)t));
             if (g.image)
                 for (uint32_t t = 0; t < mv.ntri; t += kBatchNewlineChunk) bn.push_back(make_int2((int)d, (int)t));
             local += mv.ntri;
@@ -326,6 +327,7 @@ BatchDev dev_view(sloth_batch *b)
     d.overflow = b->overflow;
     d.queue = b->queue;
     d.depth_cull = sloth_ctx_depth_cull(b->ctx);
+    d.tpb = b->tpb;
     return d;
 }
 
@@ -664,6 +666,32 @@ sloth_status sloth_batch_set_tile_shape(sloth_batch *b, int shape)
     return shape == b->shape ? SLOTH_OK : build(b, shape);
 }
 
+sloth_status sloth_batch_set_triangles_per_block(sloth_batch *b, int tpb)
+{
+    if (!b || !b->ctx || !valid_triangles_per_block(tpb)) return SLOTH_ERR_INVALID_ARGUMENT;
+    BCU(b, cudaSetDevice(b->device));
+    BCU(b, cudaStreamSynchronize(b->stream));
+    if (tpb == b->tpb) return SLOTH_OK;
+    b->tpb = tpb;
+    // the triangle block table steps by tpb: rebuild it
+    std::vector<int2> bt;
+    for (const sloth_frame_desc &fd : b->frames)
+        for (uint32_t k = 0; k < fd.ndraws; ++k) {
+            const uint32_t d = fd.first_draw + k;
+            const uint32_t ntri = sloth_mesh_view(b->meshes[d]).ntri;
+            for (uint32_t t = 0; t < ntri; t += (uint32_t)tpb) bt.push_back(make_int2((int)d, (int)t));
+        }
+    bfree(b->blk[1]);
+    b->nblk[1] = (uint32_t)bt.size();
+    BCU(b, balloc(&b->blk[1], bt.size()));
+    if (!bt.empty()) BCU(b, cudaMemcpy(b->blk[1], bt.data(), bt.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return SLOTH_OK;
+}
+
 sloth_status sloth_batch_set_persistent(sloth_batch *b, int persistent)
 {
     if (!b || !b->ctx) return SLOTH_ERR_INVALID_ARGUMENT;
@@ -699,7 +727,45 @@ sloth_status sloth_batch_set_direct_samples(sloth_batch *b, int samples)
 // Candidate sample limits of the direct path the autotuner tries (0: every triangle binned).
 static const int kDirectCandidates[] = {0, 4, 16, 64};
 
-sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, int *best_direct, float *best_ms)
+namespace {
+
+// The batch's tuning state: (tile shape, direct limit, triangles per block, persistent).
+struct BatchTune {
+    int shape, direct, tpb, persistent;
+};
+
+sloth_status apply_tune(sloth_batch *b, const BatchTune &t)
+{
+    sloth_status st = sloth_batch_set_tile_shape(b, t.shape);
+    if (st == SLOTH_OK) st = sloth_batch_set_direct_samples(b, t.direct);
+    if (st == SLOTH_OK) st = sloth_batch_set_triangles_per_block(b, t.tpb);
+    if (st == SLOTH_OK) st = sloth_batch_set_persistent(b, t.persistent);
+    return st;
+}
+
+// Mean render time (ms) of `reps` graph replays with the given settings.
+sloth_status time_tune(sloth_batch *b, const BatchTune &t, int reps, cudaEvent_t e0, cudaEvent_t e1, float *ms)
+{
+    sloth_status st = apply_tune(b, t);
+    if (st == SLOTH_OK) st = sloth_batch_render(b);     // plan + size the entries
+    if (st == SLOTH_OK) st = settle(b);
+    if (st == SLOTH_OK) st = sloth_batch_render(b);     // capture + warm
+    if (st == SLOTH_OK) st = settle(b);
+    if (st != SLOTH_OK) return st;
+    BCU(b, cudaEventRecord(e0, b->stream));
+    for (int i = 0; i < reps && st == SLOTH_OK; ++i) st = sloth_batch_render(b);
+    BCU(b, cudaEventRecord(e1, b->stream));
+    BCU(b, cudaEventSynchronize(e1));
+    if (st != SLOTH_OK) return st;
+    BCU(b, cudaEventElapsedTime(ms, e0, e1));
+    *ms /= (float)reps;
+    return SLOTH_OK;
+}
+
+}  // namespace
+
+sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, int *best_direct, int *best_tpb,
+                                  int *best_persistent, float *best_ms)
 {
     if (!b || !b->ctx) return SLOTH_ERR_INVALID_ARGUMENT;
     if (reps < 1) reps = 3;
@@ -707,40 +773,40 @@ sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, int
     cudaEvent_t e0, e1;
     BCU(b, cudaEventCreate(&e0));
     BCU(b, cudaEventCreate(&e1));
-    int best = -1, bestd = 0;
-    float best_t = 0.0f;
-    sloth_status st = SLOTH_OK;
-    for (int shape = 0; shape < kNumTileShapes && st == SLOTH_OK; ++shape) {
-        for (int dm : kDirectCandidates) {
-            st = sloth_batch_set_tile_shape(b, shape);
-            if (st == SLOTH_OK) st = sloth_batch_set_direct_samples(b, dm);
-            if (st == SLOTH_OK) st = sloth_batch_render(b);     // plan + size the entries
-            if (st == SLOTH_OK) st = settle(b);
-            if (st == SLOTH_OK) st = sloth_batch_render(b);     // capture + warm
-            if (st == SLOTH_OK) st = settle(b);
-            if (st != SLOTH_OK) break;
-            cudaEventRecord(e0, b->stream);
-            for (int i = 0; i < reps; ++i) sloth_batch_render(b);
-            cudaEventRecord(e1, b->stream);
-            cudaEventSynchronize(e1);
-            float ms = 0.0f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            ms /= (float)reps;
-            if (best < 0 || ms < best_t) {
-                best = shape;
-                bestd = dm;
-                best_t = ms;
+    // coordinate descent from the current settings: each dimension in turn, twice over
+    BatchTune best{b->shape, b->direct_max, b->tpb, b->persistent ? 1 : 0};
+    float best_t = -1.0f;
+    sloth_status st = time_tune(b, best, reps, e0, e1, &best_t);
+    for (int round = 0; round < 2 && st == SLOTH_OK; ++round) {
+        for (int dim = 0; dim < 4 && st == SLOTH_OK; ++dim) {
+            const int n = dim == 0 ? kNumTileShapes : dim == 1 ? 4 : dim == 2 ? 3 : 2;
+            BatchTune keep = best;
+            for (int k = 0; k < n && st == SLOTH_OK; ++k) {
+                BatchTune t = keep;
+                if (dim == 0) t.shape = k;
+                if (dim == 1) t.direct = kDirectCandidates[k];
+                if (dim == 2) t.tpb = kTrianglesPerBlockChoices[k];
+                if (dim == 3) t.persistent = k;
+                if (t.shape == keep.shape && t.direct == keep.direct && t.tpb == keep.tpb &&
+                    t.persistent == keep.persistent)
+                    continue;
+                float ms = 0.0f;
+                st = time_tune(b, t, reps, e0, e1, &ms);
+                if (st == SLOTH_OK && ms < best_t) {
+                    best = t;
+                    best_t = ms;
+                }
             }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (st == SLOTH_OK) st = apply_tune(b, best);
     if (st != SLOTH_OK) return st;
-    st = sloth_batch_set_tile_shape(b, best);
-    if (st == SLOTH_OK) st = sloth_batch_set_direct_samples(b, bestd);
-    if (st != SLOTH_OK) return st;
-    if (best_shape) *best_shape = best;
-    if (best_direct) *best_direct = bestd;
+    if (best_shape) *best_shape = best.shape;
+    if (best_direct) *best_direct = best.direct;
+    if (best_tpb) *best_tpb = best.tpb;
+    if (best_persistent) *best_persistent = best.persistent;
     if (best_ms) *best_ms = best_t;
     return SLOTH_OK;
 }

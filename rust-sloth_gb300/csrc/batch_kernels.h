@@ -47,6 +47,7 @@ struct BatchDev {
     uint32_t *overflow;        // set when the entries outgrew their capacity
     uint32_t *queue;           // the persistent raster's next item (zeroed by the item kernel)
     int depth_cull;
+    int tpb;                   // triangles per setup/fill block (the triangle block table's step)
 };
 
 // Block tables: one int2 (item, start) per block, built on the host.
@@ -61,7 +62,6 @@ cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, bool persiste
 cudaError_t launch_batch_resolve(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s);
 cudaError_t prepare_batch_kernels();
 
-constexpr uint32_t kBatchSetupBlock = 256;      // triangles per setup/fill block
 constexpr uint32_t kBatchNewlineChunk = 8192;   // triangles per newline block
 constexpr uint32_t kBatchResolveChunk = 2048;   // cells per resolve block
 

@@ -193,7 +193,7 @@ bin_items_kernel(uint32_t n, FrameGeom g, FrameBuffers fb, BinBuffers bb)
 }
 
 // One thread per triangle of the draw: small triangles write their tile entries.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kMaxTrianglesPerBlock)
 bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -242,10 +242,11 @@ cudaError_t launch_bin_items(uint32_t ntiles, const FrameGeom &g, const FrameBuf
 }
 
 cudaError_t launch_bin_fill(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
-                            const FrameBuffers &fb, const BinBuffers &bb, cudaStream_t s)
+                            const FrameBuffers &fb, const BinBuffers &bb, cudaStream_t s, int tpb)
 {
     if (ntri == 0) return cudaSuccess;
-    bin_fill_kernel<<<(ntri + 255) / 256, 256, 0, s>>>(ntri, tri_base, g, fb, bb);
+    if (!valid_triangles_per_block(tpb)) return cudaErrorInvalidValue;
+    bin_fill_kernel<<<(ntri + tpb - 1) / tpb, tpb, 0, s>>>(ntri, tri_base, g, fb, bb);
     return cudaGetLastError();
 }
 

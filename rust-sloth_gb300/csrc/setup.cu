@@ -62,7 +62,7 @@ __device__ __forceinline__ float4 transform_vertex(const MeshDev &mesh, const Ma
 
 // tv null (soups): each thread transforms its triangle's three vertices itself, which
 // saves the vertex kernel and its round trip through memory.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kMaxTrianglesPerBlock)
 setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_base, FrameGeom g,
              FrameBuffers fb, BinBuffers bb)
 {
@@ -211,10 +211,11 @@ cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *
 
 cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, uint32_t tri_base,
                          const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
-                         cudaStream_t s)
+                         cudaStream_t s, int tpb)
 {
     if (mesh.ntri == 0) return cudaSuccess;
-    setup_kernel<<<(mesh.ntri + 255) / 256, 256, 0, s>>>(mesh, tv, M, tri_base, g, fb, bb);
+    if (!valid_triangles_per_block(tpb)) return cudaErrorInvalidValue;
+    setup_kernel<<<(mesh.ntri + tpb - 1) / tpb, tpb, 0, s>>>(mesh, tv, M, tri_base, g, fb, bb);
     return cudaGetLastError();
 }
 

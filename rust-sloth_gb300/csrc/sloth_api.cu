@@ -95,6 +95,7 @@ struct sloth_ctx {
     int depth_cull = 1;
     int tile_shape = 0;
     int direct_max = 0;            // SLOTH_OPTION_DIRECT_SAMPLES (applied at the next clear)
+    int tpb = kDefaultTrianglesPerBlock;   // SLOTH_OPTION_TRIANGLES_PER_BLOCK
     bool keys_current = false;     // every tile's keys cleared for the current generation
     bool timing = false;
     std::map<std::string, KernelClock> clocks;
@@ -890,7 +891,7 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     // indexed meshes share vertices: transformed once by the vertex kernel; soups in setup
     const float4 *tv = mesh->idx ? ctx->tv : nullptr;
     if (tv) CU(ctx, timed(ctx, "vertex", [&] { return launch_vertex_transform(md, M, ctx->tv, s); }));
-    CU(ctx, timed(ctx, "setup", [&] { return launch_setup(md, tv, M, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+    CU(ctx, timed(ctx, "setup", [&] { return launch_setup(md, tv, M, ctx->tri_base, g, ctx->fb, ctx->bb, s, ctx->tpb); }));
     // the newline fold reads the records and feeds only the resolve: on its own stream,
     // beside the binning kernels
     CU(ctx, cudaEventRecord(ctx->setup_ev, s));
@@ -916,7 +917,9 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
         CU(ctx, timed(ctx, "bin_fill_large", [&] { return launch_bin_fill_large(ctx->tri_base, g, ctx->fb, ctx->bb, ctx->aux); },
                       ctx->aux));
         CU(ctx, cudaEventRecord(ctx->aux_ev, ctx->aux));
-        CU(ctx, timed(ctx, "bin_fill", [&] { return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+        CU(ctx, timed(ctx, "bin_fill", [&] {
+               return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s, ctx->tpb);
+           }));
         CU(ctx, cudaStreamWaitEvent(s, ctx->aux_ev, 0));
         size_t icap = ctx->bb.item_capacity;
         sloth_status st2;
@@ -976,6 +979,12 @@ sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value)
         if (value != 0 && value != 1) return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "depth cull is 0 or 1");
         ctx->depth_cull = (int)value;
         return SLOTH_OK;
+    case SLOTH_OPTION_TRIANGLES_PER_BLOCK:
+        if (!valid_triangles_per_block(value))
+            return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "triangles per block %lld is not 128, 256 or 512",
+                        (long long)value);
+        ctx->tpb = (int)value;
+        return SLOTH_OK;
     case SLOTH_OPTION_DIRECT_SAMPLES:
         if (value < 0 || value > SLOTH_MAX_DIRECT_SAMPLES)
             return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "direct samples %lld outside 0..%d", (long long)value,
@@ -985,6 +994,78 @@ sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value)
     default:
         return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "unknown option %d", option);
     }
+}
+
+// Candidate direct-sample limits of the single-frame autotuner.
+static const int kCtxDirectCandidates[] = {0, 4, 16, 64};
+
+sloth_status sloth_ctx_autotune(sloth_ctx *ctx, const sloth_mesh *const *meshes, const float *transforms,
+                                uint32_t ndraws, int reps, int *best_shape, int *best_direct, int *best_tpb,
+                                float *best_ms)
+{
+    if (!ctx || (ndraws && (!meshes || !transforms))) return SLOTH_ERR_INVALID_ARGUMENT;
+    if (ctx->req_w == 0 || ctx->req_h == 0)
+        return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "no viewport: call sloth_ctx_set_viewport first");
+    if (reps < 1) reps = 3;
+    CU(ctx, cudaSetDevice(ctx->device));
+    const int shape0 = ctx->tile_shape, direct0 = ctx->direct_max, tpb0 = ctx->tpb;
+    const bool timing0 = ctx->timing;
+    ctx->timing = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CU(ctx, cudaEventCreate(&e0));
+    CU(ctx, cudaEventCreate(&e1));
+    auto frame = [&]() -> sloth_status {
+        sloth_status st = sloth_ctx_clear(ctx);
+        for (uint32_t i = 0; i < ndraws && st == SLOTH_OK; ++i) st = sloth_draw_mesh(ctx, meshes[i], transforms + 16 * i);
+        if (st == SLOTH_OK) st = resolve_pending(ctx);
+        return st;
+    };
+    int bs = shape0, bd = direct0, bt = tpb0;
+    float best = -1.0f;
+    sloth_status st = SLOTH_OK;
+    for (int shape = 0; shape < kNumTileShapes && st == SLOTH_OK; ++shape)
+        for (int direct : kCtxDirectCandidates)
+            for (int tpb : kTrianglesPerBlockChoices) {
+                if (st != SLOTH_OK) break;
+                ctx->tile_shape = shape;
+                ctx->direct_max = direct;
+                ctx->tpb = tpb;
+                st = frame();                          // sizes buffers for this setting
+                if (st == SLOTH_OK) st = sloth_ctx_synchronize(ctx);
+                if (st == SLOTH_OK) st = frame();      // warm
+                if (st != SLOTH_OK) break;
+                cudaEventRecord(e0, ctx->stream);
+                for (int r = 0; r < reps && st == SLOTH_OK; ++r) st = frame();
+                cudaEventRecord(e1, ctx->stream);
+                if (st == SLOTH_OK) st = sloth_ctx_synchronize(ctx);
+                float ms = 0.0f;
+                if (st == SLOTH_OK && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) {
+                    ms /= (float)reps;
+                    if (best < 0.0f || ms < best) {
+                        best = ms;
+                        bs = shape;
+                        bd = direct;
+                        bt = tpb;
+                    }
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->timing = timing0;
+    if (st != SLOTH_OK) {
+        ctx->tile_shape = shape0;
+        ctx->direct_max = direct0;
+        ctx->tpb = tpb0;
+        return st;
+    }
+    ctx->tile_shape = bs;
+    ctx->direct_max = bd;
+    ctx->tpb = bt;
+    if (best_shape) *best_shape = bs;
+    if (best_direct) *best_direct = bd;
+    if (best_tpb) *best_tpb = bt;
+    if (best_ms) *best_ms = best;
+    return SLOTH_OK;
 }
 
 sloth_status sloth_ctx_set_timing(sloth_ctx *ctx, int enable)

@@ -95,6 +95,13 @@ struct Mat4 {
     float m[16];             // row-major
 };
 
+// Triangles per block of the setup and fill kernels (one thread per triangle): a tuning
+// choice, the results do not depend on it.
+constexpr int kDefaultTrianglesPerBlock = 256;
+constexpr int kMaxTrianglesPerBlock = 512;
+constexpr int kTrianglesPerBlockChoices[3] = {128, 256, 512};
+inline bool valid_triangles_per_block(long long v) { return v == 128 || v == 256 || v == 512; }
+
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked
 // up once per device): grids of the grid-stride kernels are sized by it.
 int device_sm_count();
@@ -114,7 +121,7 @@ cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *
 // (soups only: mesh.idx null).
 cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, uint32_t tri_base,
                          const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
-                         cudaStream_t s);
+                         cudaStream_t s, int tpb = kDefaultTrianglesPerBlock);
 // newline sentinels (image mode): fold each triangle's row range into the segment tree.
 cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
                            const FrameBuffers &fb, cudaStream_t s);
@@ -124,7 +131,8 @@ cudaError_t launch_bin_scan(uint32_t ntiles, const BinBuffers &bb, cudaStream_t 
 cudaError_t launch_bin_items(uint32_t ntiles, const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
                              cudaStream_t s);
 cudaError_t launch_bin_fill(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
-                            const FrameBuffers &fb, const BinBuffers &bb, cudaStream_t s);
+                            const FrameBuffers &fb, const BinBuffers &bb, cudaStream_t s,
+                            int tpb = kDefaultTrianglesPerBlock);
 cudaError_t launch_bin_fill_large(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
                                   const BinBuffers &bb, cudaStream_t s);
 

@@ -25,6 +25,7 @@ OPTION_DEPTH_CULL = 1
 OPTION_TILE_SHAPE = 2
 OPTION_WAIT_TEST = 3
 OPTION_DIRECT_SAMPLES = 4
+OPTION_TRIANGLES_PER_BLOCK = 5
 STATUS ={0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "CUDA", 4: "LIMIT", 5: "DEVICE_FAULT"}
 
 # Every symbol declared in include/sloth_gpu.h, with (restype, argtypes).
@@ -60,6 +61,8 @@ SIGNATURES = {
     "sloth_mesh_update": (C.c_int, [_vp, _f32p, _f32p, _f32p, _u8p]),
     "sloth_draw_mesh": (C.c_int, [_vp, _vp, _f32p]),
     "sloth_ctx_set_option": (C.c_int, [_vp, C.c_int, C.c_int64]),
+    "sloth_ctx_autotune": (C.c_int, [_vp, C.POINTER(_vp), _f32p, C.c_uint32, C.c_int, C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)]),
     "sloth_render_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_uint32, _vp, _f32p, C.c_uint32, C.c_uint32,
                                        C.c_int, _vp, _vp, _vp, _vp]),
     "sloth_tile_shape": (C.c_int, [C.c_int, _u32p, _u32p]),
@@ -71,7 +74,9 @@ SIGNATURES = {
     "sloth_batch_frame_buffers": (C.c_int, [_vp, C.c_uint32, C.POINTER(_vp), C.POINTER(_vp)]),
     "sloth_batch_fragments": (C.c_int, [_vp, _u64p]),
     "sloth_batch_set_tile_shape": (C.c_int, [_vp, C.c_int]),
-    "sloth_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+    "sloth_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+    "sloth_batch_set_triangles_per_block": (C.c_int, [_vp, C.c_int]),
     "sloth_batch_set_direct_samples": (C.c_int, [_vp, C.c_int]),
     "sloth_batch_set_persistent": (C.c_int, [_vp, C.c_int]),
     "sloth_batch_depth_cells": (C.c_int, [_vp, C.c_uint32, _u64p, _u64p]),
@@ -262,6 +267,20 @@ class Context:
         straight into the depth keys by setup (same results); applies at the next clear."""
         self._check(self.lib.sloth_ctx_set_option(self.h, OPTION_DIRECT_SAMPLES, samples))
 
+    def set_triangles_per_block(self, tpb: int):
+        """SLOTH_OPTION_TRIANGLES_PER_BLOCK: 128, 256 or 512 threads per setup/fill block."""
+        self._check(self.lib.sloth_ctx_set_option(self.h, OPTION_TRIANGLES_PER_BLOCK, tpb))
+
+    def autotune(self, draws, reps: int = 3) -> dict:
+        """sloth_ctx_autotune over draws [(Mesh, transform), ...]: the fastest (tile shape,
+        direct limit, triangles per block), now the context's options, and its frame time."""
+        arr = (C.c_void_p * max(1, len(draws)))(*[m.h for m, _ in draws])
+        mats = np.ascontiguousarray(np.stack([_mat(t) for _, t in draws]) if draws else np.zeros(16, np.float32))
+        s, d, t, ms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        self._check(self.lib.sloth_ctx_autotune(self.h, arr, _ptr(mats, C.c_float), len(draws), reps, C.byref(s),
+                                                C.byref(d), C.byref(t), C.byref(ms)))
+        return {"shape": s.value, "direct": d.value, "tpb": t.value, "ms": ms.value}
+
     def set_timing(self, on: bool):
         self._check(self.lib.sloth_ctx_set_timing(self.h, 1 if on else 0))
 
@@ -431,11 +450,16 @@ class Batch:
         """Persistent raster over the device-side item queue (default) or one CTA per item."""
         self.ctx._check(self.lib.sloth_batch_set_persistent(self.h, 1 if on else 0))
 
-    def autotune(self, reps: int = 3):
-        """(tile shape, direct-sample limit, mean render ms) of the fastest pair, now set."""
-        s, d, ms = C.c_int(), C.c_int(), C.c_float()
-        self.ctx._check(self.lib.sloth_batch_autotune(self.h, reps, C.byref(s), C.byref(d), C.byref(ms)))
-        return s.value, d.value, ms.value
+    def set_triangles_per_block(self, tpb: int):
+        self.ctx._check(self.lib.sloth_batch_set_triangles_per_block(self.h, tpb))
+
+    def autotune(self, reps: int = 3) -> dict:
+        """The fastest (tile shape, direct limit, triangles per block, persistent) setting,
+        now set, and its mean render time."""
+        s, d, t, p, ms = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        self.ctx._check(self.lib.sloth_batch_autotune(self.h, reps, C.byref(s), C.byref(d), C.byref(t), C.byref(p),
+                                                      C.byref(ms)))
+        return {"shape": s.value, "direct": d.value, "tpb": t.value, "persistent": bool(p.value), "ms": ms.value}
 
     def flush(self, frame: int, fmt: int = 1) -> bytes:
         """Context::flush's stdout bytes for one frame, formatted on the GPU."""

@@ -93,8 +93,13 @@ def test_batch_every_tile_shape_and_autotune(ctx):
         b.set_direct_samples(direct)
         b.render()
         check_frames(b, meshes, frames, f"direct {direct}")
-    best, direct, ms = b.autotune(reps=2)
-    assert 0 <= best < len(S.tile_shapes()) and direct in (0, 4, 16, 64) and ms > 0
+    for tpb in (128, 512):
+        b.set_triangles_per_block(tpb)
+        b.render()
+        check_frames(b, meshes, frames, f"{tpb} triangles per block")
+    best = b.autotune(reps=2)
+    assert 0 <= best["shape"] < len(S.tile_shapes()) and best["direct"] in (0, 4, 16, 64)
+    assert best["tpb"] in (128, 256, 512) and best["ms"] > 0
     b.render()
     check_frames(b, meshes, frames, "autotuned")
     b.close()
@@ -119,6 +124,43 @@ def test_batch_entry_overflow_replans(ctx):
     for i in range(3):
         assert_same((*b.read(i), None), ref, f"overflow frame {i}")
     b.close()
+
+
+@pytest.mark.parametrize("direct,tpb", [(0, 128), (16, 512), (4, 256)])
+def test_context_tuning_settings(ctx, direct, tpb):
+    """Every value of the autotuner's other dimensions renders the same frame."""
+    m = W.soup(6000, seed=52, n_large=15)
+    R = O.euler_rotation(*W.cli_rotation(yaw=0.2, pitch=0.4))
+    ctx.set_triangles_per_block(tpb)
+    try:
+        ctx.set_direct_samples(direct)
+        ctx.set_depth_cull(True)
+        for w, h, image in [(321, 181, True), (200, 90, False)]:
+            U = O.viewport_transform(w, h, 0.75)
+            ref = oracle_render([m], R, w, h, image, U=U)
+            assert_same(gpu_render(ctx, [m], R, w, h, image, U=U, depth_cull=True), ref, f"{direct}/{tpb} {w}x{h}")
+    finally:
+        ctx.set_triangles_per_block(256)
+        ctx.set_direct_samples(0)
+
+
+def test_context_autotune_renders_the_same_frame(ctx):
+    m = W.soup(8000, seed=53, n_large=20)
+    R = O.euler_rotation(*W.cli_rotation(yaw=1.1))
+    dm = dev_mesh(ctx, m)
+    w, h = 480, 270
+    ctx.set_viewport(w, h, True)
+    ctx.update([dm])
+    best = ctx.autotune([(dm, R)], reps=2)
+    assert 0 <= best["shape"] < len(S.tile_shapes()) and best["direct"] in (0, 4, 16, 64)
+    assert best["tpb"] in (128, 256, 512) and best["ms"] > 0
+    ctx.clear()
+    ctx.draw_mesh(dm, R)
+    cells, z, winner = ctx.read()
+    assert_same((cells, z, winner, None), oracle_render([m], R, w, h, True), "autotuned context")
+    ctx.set_tile_shape(0)
+    ctx.set_direct_samples(0)
+    ctx.set_triangles_per_block(256)
 
 
 @pytest.mark.parametrize("shape", range(5))
