@@ -186,7 +186,11 @@ def test_depth_culling_skips_hidden_fragments(ctx):
     R = O.euler_rotation(*W.cli_rotation())
     w, h = 480, 270
     ref = oracle_render([m], R, w, h, True)
-    assert_same(gpu_render(ctx, [m], R, w, h, True, depth_cull=True), ref, "dense soup")
+    # the first frame may outgrow the entry buffer an earlier test sized (the draw does not
+    # wait for its count): it is then rasterized by the unculled fallback, and the next
+    # draw grows the buffer
+    for _ in range(2):
+        assert_same(gpu_render(ctx, [m], R, w, h, True, depth_cull=True), ref, "dense soup")
     ctx.set_depth_cull(True)
     assert ctx.fragments() < 0.75 * ref.fragments
 
