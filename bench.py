@@ -531,8 +531,9 @@ CONFIG3 = ("config3: 256 views of a displaced icosphere (subdivision 6, 81,920 t
            "+ 64 soups with log-uniform triangle counts 1k-500k at viewports 80x24..1920x1080, image mode")
 
 
-def config3_frames(seed: int = 3):
-    """Host meshes and frame specs of config 3 (one mesh per frame)."""
+def config3_frames(seed: int = 3, views: int = 256, soups: int = 64):
+    """Host meshes and frame specs of config 3 (one mesh per frame); fewer views and soups
+    (the first ones of the same seeded sequence) give a smaller case for profiling."""
     import workloads as W
     from oracle import oracle as O
     rng = np.random.default_rng(seed)
@@ -540,13 +541,14 @@ def config3_frames(seed: int = 3):
     meshes = [ico]
     frames = []
     ext = O.scene_extent([ico["bbox_max"]])
-    for _ in range(256):
+    for k in range(256):
         theta = float(rng.uniform(0.0, 2.0 * np.pi))
         R = O.euler_rotation(*W.cli_rotation(pitch=theta))     # turntable axis
-        frames.append((0, 640, 360, True, O.viewport_transform(640, 360, ext), R))
+        if k < views:
+            frames.append((0, 640, 360, True, O.viewport_transform(640, 360, ext), R))
     sizes = [(80, 24), (160, 48), (640, 360), (1920, 1080)]
     counts = np.exp(rng.uniform(np.log(1e3), np.log(5e5), size=64)).astype(int)
-    for i, n in enumerate(counts):
+    for i, n in enumerate(counts[:soups]):
         m = W.soup(int(n), seed=1000 + i, n_large=max(1, int(n) // 500))
         meshes.append(m)
         w, h = sizes[int(rng.integers(0, 4))]
@@ -560,7 +562,7 @@ def run_config3(torch, stream, device, args):
     and through the plain per-frame path (clear + draw_mesh + resolve per frame, one
     context per viewport size), both timed with CUDA events on the same stream."""
     import sloth_gpu as S
-    meshes, specs = config3_frames()
+    meshes, specs = config3_frames(views=args.c3_views, soups=args.c3_soups)
     ctx = S.Context(device, stream=stream.cuda_stream)
     dev = [S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"], m["idx"], m["bbox_max"]) for m in meshes]
     frames = [{"w": w, "h": h, "image": im, "U": U, "draws": [(dev[mi], R)]} for mi, w, h, im, U, R in specs]
@@ -598,6 +600,8 @@ def run_config3(torch, stream, device, args):
     batched_ms = forms[tuned["persistent"]]
 
     plain = {}
+    if args.no_plain:
+        plain_ms = float("nan")
     def plain_pass():
         for f in frames:
             key = (f["w"], f["h"], f["image"])
@@ -614,15 +618,16 @@ def run_config3(torch, stream, device, args):
             for m, R in f["draws"]:
                 c.draw_mesh(m, R)
             c.device_buffers()
-    plain_pass()
-    torch.cuda.synchronize()
-    psteps = max(2, steps // 4)
-    a.record(stream)
-    for _ in range(psteps):
+    if not args.no_plain:
         plain_pass()
-    b.record(stream)
-    torch.cuda.synchronize()
-    plain_ms = a.elapsed_time(b) / psteps
+        torch.cuda.synchronize()
+        psteps = max(2, steps // 4)
+        a.record(stream)
+        for _ in range(psteps):
+            plain_pass()
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = a.elapsed_time(b) / psteps
 
     # every batched frame (the last timed render) against the oracle, bit for bit
     par = None
@@ -857,6 +862,9 @@ def main():
                     help="tile shape of the config-3 batch (default: autotuned with the direct limit)")
     ap.add_argument("--batched-direct", type=int, default=0,
                     help="direct-sample limit of the config-3 batch when --batched-shape fixes the shape")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-frame pass of the config-3 leg")
+    ap.add_argument("--c3-views", type=int, default=256, help="icosphere views of config 3 (a smaller case)")
+    ap.add_argument("--c3-soups", type=int, default=64, help="soup frames of config 3 (a smaller case)")
     ap.add_argument("--batched-tpb", type=int, default=256,
                     help="triangles per setup/fill block of the config-3 batch when --batched-shape fixes the shape")
     ap.add_argument("--only-diff", action="store_true", help="run only the differentiable legs (configs 4 and 5)")

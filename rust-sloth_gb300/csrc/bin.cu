@@ -171,12 +171,25 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
 
 // One thread per tile: the raster items (tile, slice) of the tile, and for a tile that is
 // rasterized in slices, its keys cleared (unless they hold keys of earlier draws since
-// the clear) and its generation set before the slices fold into them.
+// the clear) and its generation set before the slices fold into them.  When the draw's
+// entries outgrew the buffer (the raster folds its triangles without tiles), every tile
+// gets that treatment instead.
 __global__ void __launch_bounds__(256)
 bin_items_kernel(uint32_t n, FrameGeom g, FrameBuffers fb, BinBuffers bb)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
+    if (bb.tile_offset[n] > bb.capacity) {
+        if (fb.tile_gen[t] != fb.gen) {
+            const int tr = (int)t / g.ntx, tc = (int)t - tr * g.ntx;
+            unsigned long long *k0 = reinterpret_cast<unsigned long long *>(fb.keys) +
+                                     (size_t)tr * g.th * g.pitch + (size_t)tc * g.tw;
+            for (int r = 0; r < g.th; ++r)
+                for (int c = 0; c < g.tw; ++c) k0[(size_t)r * g.pitch + c] = kEmptyKey;
+            fb.tile_gen[t] = fb.gen;
+        }
+        return;
+    }
     const SplitParams sp = split_params(bb, n);
     const uint32_t cnt = bb.tile_count[t], ns = tile_slices(cnt, sp);
     const bool split = cnt > sp.threshold;

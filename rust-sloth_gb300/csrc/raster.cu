@@ -5,56 +5,15 @@
 
 namespace sloth {
 
-// One CTA per raster item (tile, slice); CTAs past the item count return at once.
-template <int TW, int TH>
-__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks)
-raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb, uint32_t ntiles, int depth_cull)
+// Overflow fallback of a draw whose tile entries outgrew the entry buffer (its fill wrote
+// what fitted): one warp per triangle of the draw (grid-stride over the raster grid's
+// warps); a triangle the tiles would have rasterized (not culled, not direct) has every
+// sample of its range tested, the lanes striding over the range, and its covered samples'
+// keys folded into the global keys with a 64-bit atomicMin -- the same minimum as the tile
+// raster's.  bin_items_kernel has made every tile's keys current before.
+__device__ __forceinline__ void overflow_fold(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
+                                              const FrameBuffers &fb)
 {
-    __shared__ TileSmem<TW, TH> S;
-    if (blockIdx.x >= bb.slice_offset[ntiles] || blockIdx.x >= bb.item_capacity) return;
-    if (bb.tile_offset[ntiles] > bb.capacity) return;   // entries past the buffer: launch_overflow does it
-    const uint2 it = bb.items[blockIdx.x];
-    const uint32_t all = bb.tile_count[it.x];
-    const uint32_t thr = bb.slice_offset[ntiles + 1], slice = bb.slice_offset[ntiles + 2];
-    const bool split = all > thr;
-    const uint32_t first = split ? it.y * slice : 0u;
-    const uint32_t cnt = split ? min(slice, all - first) : all;
-    raster_barrier_init(S);
-    uint32_t phase = 0;
-    raster_tile<TW, TH>(S, g, fb, (int)it.x, cnt, bb.entries + bb.tile_offset[it.x] + first, depth_cull, phase,
-                        split);
-}
-
-// Overflow fallback, step 1: grid-stride over tiles, one warp per tile; a tile whose keys
-// belong to an older generation gets empty keys and the current generation.
-__global__ void __launch_bounds__(256) overflow_tiles_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb,
-                                                             uint32_t ntiles)
-{
-    if (bb.tile_offset[ntiles] <= bb.capacity) return;
-    const int lane = threadIdx.x & 31;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += nwarps) {
-        if (fb.tile_gen[t] == fb.gen) continue;
-        const int tr = (int)t / g.ntx, tc = (int)t - tr * g.ntx;
-        unsigned long long *k0 = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)tr * g.th * g.pitch +
-                                 (size_t)tc * g.tw;
-        for (int i = lane; i < g.th * g.tw; i += 32) {
-            const int r = i / g.tw, c = i - r * g.tw;
-            k0[(size_t)r * g.pitch + c] = kEmptyKey;
-        }
-        __syncwarp();
-        if (lane == 0) fb.tile_gen[t] = fb.gen;
-    }
-}
-
-// Overflow fallback, step 2: one warp per triangle of the draw (grid-stride); a triangle
-// the tiles would have rasterized (not culled, not direct) has every sample of its range
-// tested, the lanes striding over the range, and its covered samples' keys folded into the
-// global keys with a 64-bit atomicMin (the same minimum as the tile raster's).
-__global__ void __launch_bounds__(256) overflow_raster_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g,
-                                                              FrameBuffers fb, BinBuffers bb, uint32_t ntiles)
-{
-    if (bb.tile_offset[ntiles] <= bb.capacity) return;
     const int lane = threadIdx.x & 31;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(fb.keys);
@@ -83,28 +42,41 @@ __global__ void __launch_bounds__(256) overflow_raster_kernel(uint32_t ntri, uin
     add_frags_warp(frags, fb.fragments);
 }
 
-cudaError_t launch_overflow(uint32_t ntri, uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
-                            const BinBuffers &bb, cudaStream_t s)
+// One CTA per raster item (tile, slice); CTAs past the item count return at once.  When the
+// draw's entries outgrew the buffer, every CTA of the grid takes part in overflow_fold
+// instead.
+template <int TW, int TH>
+__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks)
+raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb, uint32_t ntiles, int depth_cull, uint32_t ntri,
+              uint32_t tri_base)
 {
-    const uint32_t ntiles = (uint32_t)(g.ntx * g.nty);
-    if (ntiles == 0 || ntri == 0) return cudaSuccess;
-    const int grid = 2 * device_sm_count();
-    overflow_tiles_kernel<<<grid, 256, 0, s>>>(g, fb, bb, ntiles);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    overflow_raster_kernel<<<4 * grid, 256, 0, s>>>(ntri, tri_base, g, fb, bb, ntiles);
-    return cudaGetLastError();
+    __shared__ TileSmem<TW, TH> S;
+    if (bb.tile_offset[ntiles] > bb.capacity) {
+        overflow_fold(ntri, tri_base, g, fb);
+        return;
+    }
+    if (blockIdx.x >= bb.slice_offset[ntiles] || blockIdx.x >= bb.item_capacity) return;
+    const uint2 it = bb.items[blockIdx.x];
+    const uint32_t all = bb.tile_count[it.x];
+    const uint32_t thr = bb.slice_offset[ntiles + 1], slice = bb.slice_offset[ntiles + 2];
+    const bool split = all > thr;
+    const uint32_t first = split ? it.y * slice : 0u;
+    const uint32_t cnt = split ? min(slice, all - first) : all;
+    raster_barrier_init(S);
+    uint32_t phase = 0;
+    raster_tile<TW, TH>(S, g, fb, (int)it.x, cnt, bb.entries + bb.tile_offset[it.x] + first, depth_cull, phase,
+                        split);
 }
 
 cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
-                          int depth_cull, cudaStream_t s)
+                          int depth_cull, uint32_t ntri, uint32_t tri_base, cudaStream_t s)
 {
     const uint32_t ntiles = (uint32_t)(g.ntx * g.nty);
     if (ntiles == 0) return cudaSuccess;
     const uint32_t grid = bb.item_capacity;
 #define SLOTH_RASTER_CASE(W_, H_)                                                              \
     if (g.tw == W_ && g.th == H_) {                                                            \
-        raster_kernel<W_, H_><<<grid, kRasterThreads, 0, s>>>(g, fb, bb, ntiles, depth_cull);  \
+        raster_kernel<W_, H_><<<grid, kRasterThreads, 0, s>>>(g, fb, bb, ntiles, depth_cull, ntri, tri_base); \
         return cudaGetLastError();                                                             \
     }
     SLOTH_TILE_SHAPES(SLOTH_RASTER_CASE)

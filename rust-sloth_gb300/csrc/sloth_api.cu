@@ -904,9 +904,9 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
     // The entry count is known only on the device.  With an entry buffer from earlier draws
     // the rest of the draw goes ahead with it and the host does not wait: the fill kernels
-    // write no slot past the capacity, the raster does nothing when the count is above it,
-    // and the overflow fallback then rasterizes the draw's binned triangles straight into
-    // the keys (the same keys).  The device's running maximum of the counts comes back on
+    // write no slot past the capacity, and when the count is above it the raster launch
+    // folds the draw's binned triangles straight into the keys instead of rasterizing tiles
+    // (the same keys).  The device's running maximum of the counts comes back on
     // a side stream, and a later draw grows the buffer from it (poll_entry_max).  The first
     // draw on a context, with no buffer yet, waits for its count and sizes the buffer.
     auto rest = [&](size_t entries_bound) -> sloth_status {
@@ -927,14 +927,13 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
             return st2;
         ctx->bb.item_capacity = (uint32_t)icap;
         CU(ctx, timed(ctx, "bin_items", [&] { return launch_bin_items(ntiles, g, ctx->fb, ctx->bb, s); }));
-        CU(ctx, timed(ctx, "raster", [&] { return launch_raster(g, ctx->fb, ctx->bb, ctx->depth_cull, s); }));
+        CU(ctx, timed(ctx, "raster", [&] {
+               return launch_raster(g, ctx->fb, ctx->bb, ctx->depth_cull, mesh->ntri, ctx->tri_base, s);
+           }));
         return SLOTH_OK;
     };
     if (ctx->bb.entries && ctx->bb.capacity > 0) {
         if ((st = rest(ctx->bb.capacity)) != SLOTH_OK) return st;
-        CU(ctx, timed(ctx, "overflow", [&] {
-               return launch_overflow(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s);
-           }));
         if (!ctx->max_pending) {
             CU(ctx, cudaEventRecord(ctx->scan_ev, s));
             CU(ctx, cudaStreamWaitEvent(ctx->side, ctx->scan_ev, 0));

@@ -136,17 +136,13 @@ cudaError_t launch_bin_fill(uint32_t ntri, uint32_t tri_base, const FrameGeom &g
 cudaError_t launch_bin_fill_large(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
                                   const BinBuffers &bb, cudaStream_t s);
 
-// per-tile raster: 64-bit atomicMin of depth keys in shared memory, merged into keys.
+// per-tile raster: 64-bit atomicMin of depth keys in shared memory, merged into keys.  A
+// draw whose tile entries outgrew the entry buffer (the scan total is above the capacity;
+// its fill wrote what fitted) is rasterized by the same launch without tiles: the item
+// kernel has made every tile's keys current, and one warp per binned triangle of the draw
+// (ntri triangles from tri_base) folds its covered samples straight into the global keys.
 cudaError_t launch_raster(const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb, int depth_cull,
-                          cudaStream_t s);
-
-// A draw whose tile entries outgrew the entry buffer (the scan total is above the
-// capacity; its fill wrote what fitted and its raster did nothing) is rasterized here
-// instead: every tile not yet current gets empty keys, then one warp per binned triangle
-// folds its covered samples straight into the global keys.  Both kernels return at once
-// when the entries fitted.
-cudaError_t launch_overflow(uint32_t ntri, uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
-                            const BinBuffers &bb, cudaStream_t s);
+                          uint32_t ntri, uint32_t tri_base, cudaStream_t s);
 
 // resolve: keys -> z, frame cells, winners.
 cudaError_t launch_resolve(const FrameGeom &g, const FrameBuffers &fb, cudaStream_t s);
