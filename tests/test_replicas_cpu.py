@@ -64,7 +64,8 @@ def test_reference_arm_prints_from_rank_zero_only():
     times the CPU reference on a small sample and prints one line; rank 1 exits 0."""
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
            "--master-addr=127.0.0.1", f"--master-port={free_port()}", str(ROOT / "bench.py"), "--impl",
-           "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--ref-sample-den", "8192"]
+           "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--ref-sample-den", "8192",
+           "--no-full-frame"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=str(ROOT))
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
