@@ -240,7 +240,6 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) batch_raster
     }
     const uint32_t nitems = min(b.bb.slice_offset[b.total_tiles], b.bb.item_capacity);
     if (!kPersistent && blockIdx.x >= nitems) return;
-    raster_barrier_init(S);
     uint32_t phase = 0;
     if (!kPersistent) {
         batch_raster_item<TW, TH>(S, b, blockIdx.x, phase);
@@ -255,9 +254,9 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) batch_raster
     }
 }
 
-// blocks[i] = (frame, first cell): runs of 4 frame cells per lane (resolve_run), written
-// with one 16-byte store per buffer when the frame's outputs are aligned.
-constexpr int kBatchRun = 4;
+// blocks[i] = (frame, first cell): runs of kBatchRun frame cells per lane (resolve_run),
+// written with one store per buffer when the frame's outputs are aligned.
+constexpr int kBatchRun = 2;
 static_assert(kBatchResolveChunk % (kBatchRun * 256) == 0, "whole runs, the same trip count in every warp");
 
 __global__ void __launch_bounds__(256) batch_resolve_kernel(BatchDev b, const int2 *__restrict__ blocks)

@@ -290,7 +290,7 @@ sloth_status build(sloth_batch *b, int shape)
         bf.fb.z_out = b->z + b->z_off[f];
         bf.fb.cells_out = b->cells + b->cell_off[f];
         bf.fb.winner_out = b->winner + b->z_off[f];
-        bf.vec = ((b->cell_off[f] | b->z_off[f]) & 3u) == 0;   // the buffers are 256-byte aligned
+        bf.vec = ((b->cell_off[f] | b->z_off[f]) & 1u) == 0;   // the buffers are 256-byte aligned
         bf.fb.fragments = b->fragments;
         bf.fb.error = b->error;
         bf.fb.gen = kBatchGen;

@@ -22,8 +22,8 @@ struct BatchFrame {
     uint32_t first_draw;       // the frame's first draw
     uint32_t ndraws;
     uint64_t z_off;            // first depth cell of the frame in the batch's depth-cell order
-    int32_t vec;               // the frame's outputs start on 16-byte boundaries: the resolve
-                               // writes 4 cells per store
+    int32_t vec;               // the frame's outputs start on 8-byte boundaries: the resolve
+                               // writes 2 cells per store
 };
 
 struct BatchDraw {

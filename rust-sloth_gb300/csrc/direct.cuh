@@ -32,16 +32,17 @@ __device__ __forceinline__ uint32_t direct_raster(const TriRecord &r, uint32_t g
 {
     uint32_t frags = 0;
     for (int y = r.y0; y < r.y1; ++y) {
-        const float py = (float)y;
+        const EdgeRows c = edge_rows(r, (float)y);
+        unsigned long long *rowu = keys + (size_t)y * pitch, *roww = rowu + pitch - w;
         for (int x = r.x0; x < r.xe; ++x) {
-            const EdgeVals e = eval_edges(r, (float)x, py);
+            const EdgeVals e = eval_edges_row(r, c, (float)x);
             if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
                 ++frags;
                 const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
                 if (z < kFltMax) {
+                    // unwrapped: row y, column 2x; wrapped: row y+1, column 2x-w
                     const uint32_t nw = 2 * x < w ? 1u : 0u;
-                    const int row = nw ? y : y + 1, col = nw ? 2 * x : 2 * x - w;
-                    atomicMin(keys + (size_t)row * pitch + col, (unsigned long long)make_key(z, gtri, nw));
+                    red_min_u64((nw ? rowu : roww) + 2 * x, (unsigned long long)make_key(z, gtri, nw));
                 }
             }
         }

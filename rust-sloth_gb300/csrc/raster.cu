@@ -34,7 +34,7 @@ __device__ __forceinline__ void overflow_fold(uint32_t ntri, uint32_t tri_base, 
                 if (z < kFltMax) {
                     const uint32_t nw = 2 * x < g.w ? 1u : 0u;
                     const int row = nw ? y : y + 1, col = nw ? 2 * x : 2 * x - g.w;
-                    atomicMin(keys + (size_t)row * g.pitch + col, (unsigned long long)make_key(z, gtri, nw));
+                    red_min_u64(keys + (size_t)row * g.pitch + col, (unsigned long long)make_key(z, gtri, nw));
                 }
             }
         }
@@ -62,7 +62,6 @@ raster_kernel(FrameGeom g, FrameBuffers fb, BinBuffers bb, uint32_t ntiles, int 
     const bool split = all > thr;
     const uint32_t first = split ? it.y * slice : 0u;
     const uint32_t cnt = split ? min(slice, all - first) : all;
-    raster_barrier_init(S);
     uint32_t phase = 0;
     raster_tile<TW, TH>(S, g, fb, (int)it.x, cnt, bb.entries + bb.tile_offset[it.x] + first, depth_cull, phase,
                         split);

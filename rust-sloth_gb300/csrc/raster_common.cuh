@@ -124,13 +124,15 @@ __device__ __forceinline__ TriRecord load_record(const TriRecord *__restrict__ r
 // than zb is passed over before the edge test: no depth of the triangle can beat it.
 template <int TW, int kNotWrapped>
 __device__ __forceinline__ void fold_sample(const TriRecord &r, uint32_t gtri, int x, int y, int R0, int C0,
-                                            int w, unsigned long long *skeys, uint32_t &frags, uint32_t zb)
+                                            int w, unsigned long long *skeys, uint32_t &frags, uint32_t zb,
+                                            const EdgeRows *rows = nullptr)
 {
     const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
     const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
     unsigned long long *p = &skeys[row * TW + col];
     if (zb > *(volatile const uint32_t *)(reinterpret_cast<const uint32_t *>(p) + 1)) return;
-    const EdgeVals e = eval_edges(r, (float)x, (float)y);
+    // with the row's edge terms given (a walk along one row), only the column terms remain
+    const EdgeVals e = rows ? eval_edges_row(r, *rows, (float)x) : eval_edges(r, (float)x, (float)y);
     if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
         ++frags;
         const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
@@ -253,13 +255,16 @@ __device__ __forceinline__ int rect_area(const Rect &c)
     return c.empty() ? 0 : (c.xb - c.xa) * (c.yb - c.ya);
 }
 
-// One lane walks every sample of rect c.
+// One lane walks every sample of rect c, row by row (each row's edge terms once).
 template <int TW, int kNotWrapped>
 __device__ __forceinline__ void raster_serial(const TriRecord &r, uint32_t gtri, const Rect &c, int R0, int C0,
                                               int w, unsigned long long *skeys, uint32_t &frags, uint32_t zb)
 {
-    for (int y = c.ya; y < c.yb; ++y)
-        for (int x = c.xa; x < c.xb; ++x) fold_sample<TW, kNotWrapped>(r, gtri, x, y, R0, C0, w, skeys, frags, zb);
+    for (int y = c.ya; y < c.yb; ++y) {
+        const EdgeRows rows = edge_rows(r, (float)y);
+        for (int x = c.xa; x < c.xb; ++x)
+            fold_sample<TW, kNotWrapped>(r, gtri, x, y, R0, C0, w, skeys, frags, zb, &rows);
+    }
 }
 
 // Entries whose clipped rectangles hold at most this many samples are walked by their
@@ -327,24 +332,15 @@ __device__ __forceinline__ void refresh_bounds(TileSmem<TW, TH> &S, int R0, int 
     }
 }
 
-// The tile-load barrier, initialised once per CTA before its first raster_tile (called by
-// all threads).  raster_tile keeps its phase parity in `phase` (0 after the init).
-template <int TW, int TH>
-__device__ __forceinline__ void raster_barrier_init(TileSmem<TW, TH> &S)
-{
-    if (threadIdx.x == 0) {
-        mbar_init(&S.kbar, 1);
-        fence_proxy_async_smem();
-    }
-    block_sync();
-}
-
 // Rasterize one tile of one frame: `cnt` entries at `entries`.  Called by all threads of
 // the CTA; returns after the tile's keys are stored and its generation is set, true, or
 // false when the load of an earlier draw's keys did not arrive (the tile is left as it
 // is, the error word is set, and the CTA must take no further tile).  A slice of a split
 // tile (split true) starts from empty keys and folds its keys into the tile's with a
 // global atomicMin; the tile's keys and generation were prepared before the launch.
+// `phase` carries the tile-load barrier's state across the tiles of one CTA (0 before the
+// first): bit 1 once thread 0 has initialised the barrier (at the CTA's first load),
+// bit 0 the parity of the phase the next load completes.
 template <int TW, int TH>
 __device__ __forceinline__ bool raster_tile(TileSmem<TW, TH> &S, const FrameGeom &g, const FrameBuffers &fb,
                                             int tile, uint32_t cnt, const uint64_t *__restrict__ entries,
@@ -360,8 +356,13 @@ __device__ __forceinline__ bool raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         // 16-byte aligned at both ends), completing on an mbarrier
         if (threadIdx.x < 32) {
             // warp 0: lane 0 arms the barrier for this phase, then the lanes issue one row each
-            if (threadIdx.x == 0)
+            if (threadIdx.x == 0) {
+                if (!(phase & 2u)) {
+                    mbar_init(&S.kbar, 1);
+                    fence_proxy_async_smem();
+                }
                 mbar_expect_tx(&S.kbar, (uint32_t)(TH * TW * sizeof(unsigned long long)) + (fb.wait_test ? 16u : 0u));
+            }
             __syncwarp();
             for (int rr = threadIdx.x; rr < TH; rr += 32)
                 bulk_load(&S.keys[rr * TW], gk + (size_t)rr * g.pitch, TW * sizeof(unsigned long long), &S.kbar);
@@ -369,10 +370,10 @@ __device__ __forceinline__ bool raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         block_sync();
         if (threadIdx.x == 0) {
             const uint32_t polls = fb.wait_test ? kTestWaitPolls : kWaitPolls;
-            S.kok = (mbar_wait(&S.kbar, phase, polls) || mbar_wait(&S.kbar, phase, polls)) ? 1u : 0u;
+            S.kok = (mbar_wait(&S.kbar, phase & 1u, polls) || mbar_wait(&S.kbar, phase & 1u, polls)) ? 1u : 0u;
         }
         block_sync();
-        phase ^= 1u;
+        phase = (phase ^ 1u) | 2u;
         if (!S.kok) {
             // the copy did not arrive: report it and leave the tile as it is
             if (threadIdx.x == 0 && fb.error) atomicOr(fb.error, 1u);
@@ -573,7 +574,7 @@ __device__ __forceinline__ bool raster_tile(TileSmem<TW, TH> &S, const FrameGeom
     } else {
         for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
             const int rr = i / TW, cc = i - rr * TW;
-            if (S.keys[i] != kEmptyKey) atomicMin(&gk[(size_t)rr * g.pitch + cc], S.keys[i]);
+            if (S.keys[i] != kEmptyKey) red_min_u64(&gk[(size_t)rr * g.pitch + cc], S.keys[i]);
         }
     }
     if (threadIdx.x < 32) {

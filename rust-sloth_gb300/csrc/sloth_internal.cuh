@@ -95,6 +95,32 @@ __device__ __forceinline__ EdgeVals eval_edges(const TriRecord &r, float px, flo
     return e;
 }
 
+// The same three edge values with each edge's row term fl(dx*fl(py-ay)) computed once per
+// row: edge_eval(dx, dy, ax, ay, px, py) == fsub(row, fmul(dy, fsub(px, ax))) exactly (the
+// same operations, the same order).
+struct EdgeRows {
+    float c0, c1, c2;
+};
+__device__ __forceinline__ EdgeRows edge_rows(const TriRecord &r, float py)
+{
+    return EdgeRows{fmul(r.dx0, fsub(py, r.v2y)), fmul(r.dx1, fsub(py, r.v3y)), fmul(r.dx2, fsub(py, r.v1y))};
+}
+__device__ __forceinline__ EdgeVals eval_edges_row(const TriRecord &r, const EdgeRows &c, float px)
+{
+    EdgeVals e;
+    e.w0 = fsub(c.c0, fmul(r.dy0, fsub(px, r.v2x)));
+    e.w1 = fsub(c.c1, fmul(r.dy1, fsub(px, r.v3x)));
+    e.w2 = fsub(c.c2, fmul(r.dy2, fsub(px, r.v1x)));
+    return e;
+}
+
+// 64-bit minimum into global memory without a returned value (a fire-and-forget
+// reduction: the thread does not wait for it).
+__device__ __forceinline__ void red_min_u64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("red.global.min.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 // z of src/rasterizer.rs:77-79.
 __device__ __forceinline__ float interp_z(float v1z, float dz2, float dz3, float a, float w1,
                                           float w2)
