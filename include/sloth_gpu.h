@@ -181,15 +181,16 @@ sloth_status sloth_ctx_flush_device(sloth_ctx *ctx, int format, const char **dev
  *   takes effect at the next sloth_ctx_clear.  Results are identical either way. */
 #define SLOTH_OPTION_DIRECT_SAMPLES 4
 #define SLOTH_MAX_DIRECT_SAMPLES 256
-/* SLOTH_OPTION_TRIANGLES_PER_BLOCK: triangles (threads) per block of the setup and fill
- *   kernels, 128, 256 (the default) or 512.  Results are identical either way. */
+/* SLOTH_OPTION_TRIANGLES_PER_BLOCK: triangles per block of the setup and fill kernels,
+ *   128, 256, 1024 (the default) or 4096; a block has at most 256 threads, each taking its
+ *   share of the block's triangles in turn.  Results are identical either way. */
 #define SLOTH_OPTION_TRIANGLES_PER_BLOCK 5
 sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value);
 
 /* Autotuner of the single-frame path: renders the frame clear + draw_mesh(meshes[i],
  * transforms[16*i]) for i < ndraws + resolve, `reps` times per candidate setting, and keeps
  * the fastest (tile shape, direct-sample limit in {0, 4, 16, 64}, triangles per block in
- * {128, 256, 512}) as the context's options; reports them and the mean frame time in ms
+ * {128, 256, 1024, 4096}) as the context's options; reports them and the mean frame time in ms
  * (any output may be NULL).  Needs a viewport and utransform; leaves the context with the
  * last candidate's frame drawn (clear before the next frame). */
 sloth_status sloth_ctx_autotune(sloth_ctx *ctx, const sloth_mesh *const *meshes, const float *transforms,
@@ -287,11 +288,12 @@ sloth_status sloth_batch_set_persistent(sloth_batch *batch, int persistent);
 /* Rasterize triangles of at most `samples` samples straight into the depth keys during
  * setup (SLOTH_OPTION_DIRECT_SAMPLES for a batch; a new batch takes its context's value). */
 sloth_status sloth_batch_set_direct_samples(sloth_batch *batch, int samples);
-/* Triangles per block of the batch's setup and fill kernels: 128, 256 (the default) or 512. */
+/* Triangles per block of the batch's setup and fill kernels (SLOTH_OPTION_TRIANGLES_PER_BLOCK):
+ * 128, 256, 1024 (the default) or 4096. */
 sloth_status sloth_batch_set_triangles_per_block(sloth_batch *batch, int tpb);
 /* Autotuner: times `reps` renders of the batch per candidate setting and keeps the fastest
  * (tile shape, direct-sample limit in {0, 4, 16, 64}, triangles per block in {128, 256,
- * 512}, persistent raster or not), searching one dimension at a time from the current
+ * 1024, 4096}, persistent raster or not), searching one dimension at a time from the current
  * settings, twice over; reports the choice and its mean render time in ms (any output may
  * be NULL).  Every setting renders the same frames. */
 sloth_status sloth_batch_autotune(sloth_batch *batch, int reps, int *best_shape, int *best_direct, int *best_tpb,

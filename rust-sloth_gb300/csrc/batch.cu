@@ -49,15 +49,13 @@ __global__ void __launch_bounds__(256) batch_vertex_kernel(BatchDev b, const int
                                      row_dot(&M.m[8], xs[k], ys[k], zs[k]), 0.0f);
 }
 
-// blocks[i] = (draw, first triangle; b.tpb triangles): records, small-triangle tile
-// counts, large queue, and the direct folds of the smallest triangles.
-__global__ void __launch_bounds__(kMaxTrianglesPerBlock) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
+// One triangle of draw d (every lane of the warp calls it: t >= ntri is none): record,
+// small-triangle tile counts, large queue, and the direct folds of the smallest triangles.
+__device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const BatchDraw &d, uint32_t t)
 {
-    const int2 blk = blocks[blockIdx.x];
-    const BatchDraw &d = b.draws[blk.x];
     const BatchFrame &f = b.frames[d.frame];
-    const uint32_t t = (uint32_t)blk.y + threadIdx.x;
     bool large = false, direct = false;
+    DirectWalk dw{false, 0, 0u};
     const bool live = t < d.mesh.ntri;
     TriRecord r;
     TileSpan sp{};
@@ -73,10 +71,10 @@ __global__ void __launch_bounds__(kMaxTrianglesPerBlock) batch_setup_kernel(Batc
         }
         const float4 *tv = b.tv + d.vert_off;
         r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), d.mesh.rgb + 3 * (size_t)t, f.g.w,
-                         f.g.h);
+                         f.g.h, f.g.direct_max, &dw);
         sp = tile_span(vp, r);
         store_record(f.fb.records + d.local_base + t, r, sp.ntiles);
-        direct = is_direct(r.x0, r.xe, r.y0, r.y1, f.g.direct_max);
+        direct = dw.direct;
         large = sp.large && !direct;
     }
     count_small_tiles_warp(live && !large && !direct, r, vp, sp, b.bb.tile_count + f.tile_off);
@@ -90,10 +88,21 @@ __global__ void __launch_bounds__(kMaxTrianglesPerBlock) batch_setup_kernel(Batc
     // the smallest triangles fold their samples into the frame's global keys (direct.cuh)
     if (__any_sync(0xffffffffu, direct)) {
         const uint32_t frags = direct ? direct_raster(r, d.local_base + t, f.g.w, f.g.pitch,
-                                                      reinterpret_cast<unsigned long long *>(f.fb.keys))
+                                                      reinterpret_cast<unsigned long long *>(f.fb.keys), dw.xend,
+                                                      dw.exit_mask)
                                       : 0u;
         add_frags_warp(frags, f.fb.fragments);
     }
+}
+
+// blocks[i] = (draw, first triangle): b.tpb triangles of the draw, each thread taking
+// b.tpb / blockDim.x of them in turn.
+__global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
+{
+    const int2 blk = blocks[blockIdx.x];
+    const BatchDraw &d = b.draws[blk.x];
+    for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < (uint32_t)blk.y + (uint32_t)b.tpb; t += blockDim.x)
+        batch_setup_triangle(b, d, t);
 }
 
 // blocks[i] = (draw, first triangle of a chunk): newline segment tree of the draw's frame.
@@ -144,12 +153,9 @@ __global__ void __launch_bounds__(256) batch_bin_large_kernel(BatchDev b)
     }
 }
 
-// blocks[i] = (draw, first triangle): small triangles' tile entries.
-__global__ void __launch_bounds__(kMaxTrianglesPerBlock) batch_fill_kernel(BatchDev b, const int2 *__restrict__ blocks)
+// One triangle of draw d: a small triangle's tile entries.
+__device__ __forceinline__ void batch_fill_triangle(const BatchDev &b, const BatchDraw &d, uint32_t t)
 {
-    const int2 blk = blocks[blockIdx.x];
-    const BatchDraw &d = b.draws[blk.x];
-    const uint32_t t = (uint32_t)blk.y + threadIdx.x;
     const BatchFrame &f = b.frames[d.frame];
     const uint32_t gtri = d.local_base + t;
     const Viewport vp = vp_batch(f.g);
@@ -166,6 +172,15 @@ __global__ void __launch_bounds__(kMaxTrianglesPerBlock) batch_fill_kernel(Batch
     }
     fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, b.bb.tile_cursor + f.tile_off,
                     b.bb.entries, b.bb.capacity);
+}
+
+// blocks[i] = (draw, first triangle): the setup kernel's partition.
+__global__ void __launch_bounds__(kSetupThreads, kFillMinBlocks) batch_fill_kernel(BatchDev b, const int2 *__restrict__ blocks)
+{
+    const int2 blk = blocks[blockIdx.x];
+    const BatchDraw &d = b.draws[blk.x];
+    for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < (uint32_t)blk.y + (uint32_t)b.tpb; t += blockDim.x)
+        batch_fill_triangle(b, d, t);
 }
 
 __device__ __forceinline__ uint32_t frame_of_tile(const BatchDev &b, uint32_t tile)
@@ -290,7 +305,7 @@ cudaError_t launch_batch_setup(const BatchDev &b, const int2 *blocks, uint32_t n
 {
     if (!nblocks) return cudaSuccess;
     if (!valid_triangles_per_block(b.tpb)) return cudaErrorInvalidValue;
-    batch_setup_kernel<<<nblocks, b.tpb, 0, s>>>(b, blocks);
+    batch_setup_kernel<<<nblocks, setup_block_threads(b.tpb), 0, s>>>(b, blocks);
     return cudaGetLastError();
 }
 
@@ -316,7 +331,7 @@ cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nb
 {
     if (!nblocks) return cudaSuccess;
     if (!valid_triangles_per_block(b.tpb)) return cudaErrorInvalidValue;
-    batch_fill_kernel<<<nblocks, b.tpb, 0, s>>>(b, blocks);
+    batch_fill_kernel<<<nblocks, setup_block_threads(b.tpb), 0, s>>>(b, blocks);
     return cudaGetLastError();
 }
 

@@ -779,7 +779,7 @@ sloth_status sloth_batch_autotune(sloth_batch *b, int reps, int *best_shape, int
     sloth_status st = time_tune(b, best, reps, e0, e1, &best_t);
     for (int round = 0; round < 2 && st == SLOTH_OK; ++round) {
         for (int dim = 0; dim < 4 && st == SLOTH_OK; ++dim) {
-            const int n = dim == 0 ? kNumTileShapes : dim == 1 ? 4 : dim == 2 ? 3 : 2;
+            const int n = dim == 0 ? kNumTileShapes : dim == 1 ? 4 : dim == 2 ? 4 : 2;
             BatchTune keep = best;
             for (int k = 0; k < n && st == SLOTH_OK; ++k) {
                 BatchTune t = keep;

@@ -205,11 +205,11 @@ bin_items_kernel(uint32_t n, FrameGeom g, FrameBuffers fb, BinBuffers bb)
     }
 }
 
-// One thread per triangle of the draw: small triangles write their tile entries.
-__global__ void __launch_bounds__(kMaxTrianglesPerBlock)
-bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
+// Triangles of the draw, tpb per block (setup_kernel's partition): small triangles write
+// their tile entries.
+__device__ __forceinline__ void fill_triangle(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
+                                              const FrameBuffers &fb, const BinBuffers &bb, uint32_t t)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t gtri = tri_base + t;
     const Viewport vp = vp_of(g);
     const bool live = t < ntri;
@@ -226,6 +226,14 @@ bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, 
         if (is_direct(r.x0, r.xe, r.y0, r.y1, g.direct_max)) sp.ntiles = 0;   // rasterized by setup
     }
     fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
+}
+
+__global__ void __launch_bounds__(kSetupThreads, kFillMinBlocks)
+bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb, int tpb)
+{
+    for (uint32_t t = blockIdx.x * (uint32_t)tpb + threadIdx.x; t < (blockIdx.x + 1u) * (uint32_t)tpb;
+         t += blockDim.x)
+        fill_triangle(ntri, tri_base, g, fb, bb, t);
 }
 
 static int large_grid()
@@ -259,7 +267,7 @@ cudaError_t launch_bin_fill(uint32_t ntri, uint32_t tri_base, const FrameGeom &g
 {
     if (ntri == 0) return cudaSuccess;
     if (!valid_triangles_per_block(tpb)) return cudaErrorInvalidValue;
-    bin_fill_kernel<<<(ntri + tpb - 1) / tpb, tpb, 0, s>>>(ntri, tri_base, g, fb, bb);
+    bin_fill_kernel<<<(ntri + tpb - 1) / tpb, setup_block_threads(tpb), 0, s>>>(ntri, tri_base, g, fb, bb, tpb);
     return cudaGetLastError();
 }
 

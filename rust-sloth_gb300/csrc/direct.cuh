@@ -24,18 +24,23 @@ __host__ __device__ __forceinline__ bool is_direct(int x0, int xe, int y0, int y
     return x0 < xe && y0 < y1 && (uint32_t)(xe - x0) * (uint32_t)(y1 - y0) <= (uint32_t)direct_max;
 }
 
-// Every sample of the range, in the reference's row-major order (the order does not matter
-// for the result).  Sample (x, y) writes depth cell y*w + 2x (src/rasterizer.rs:80): row y,
-// column 2x when 2x < w, else row y+1, column 2x-w.  Returns the covered samples.
+// The samples of rows [y0,y1) from column x0 to xend (exclusive) in the reference's
+// row-major order (the order does not matter for the result); a row ends early at the
+// first column where an edge of exit_mask (bit i: edge i) is negative -- edges whose value
+// only falls along the row, so no later sample of the row can be covered.  Sample (x, y)
+// writes depth cell y*w + 2x (src/rasterizer.rs:80): row y, column 2x when 2x < w, else
+// row y+1, column 2x-w.  Returns the covered samples.
 __device__ __forceinline__ uint32_t direct_raster(const TriRecord &r, uint32_t gtri, int w, int pitch,
-                                                 unsigned long long *keys)
+                                                 unsigned long long *keys, int xend, uint32_t exit_mask)
 {
     uint32_t frags = 0;
     for (int y = r.y0; y < r.y1; ++y) {
         const EdgeRows c = edge_rows(r, (float)y);
         unsigned long long *rowu = keys + (size_t)y * pitch, *roww = rowu + pitch - w;
-        for (int x = r.x0; x < r.xe; ++x) {
+        for (int x = r.x0; x < xend; ++x) {
             const EdgeVals e = eval_edges_row(r, c, (float)x);
+            const uint32_t neg = (e.w0 < 0.0f ? 1u : 0u) | (e.w1 < 0.0f ? 2u : 0u) | (e.w2 < 0.0f ? 4u : 0u);
+            if (neg & exit_mask) break;
             if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
                 ++frags;
                 const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);

@@ -7,6 +7,7 @@
 #pragma once
 
 #include "bounds.cuh"
+#include "direct.cuh"
 #include "sloth_internal.cuh"
 
 namespace sloth {
@@ -78,10 +79,25 @@ __device__ __forceinline__ void store_record(TriRecord *dst, const TriRecord &r,
     else reinterpret_cast<int4 *>(dst)[4] = make_int4(r.x0, r.xe, r.y0, r.y1);
 }
 
+// How the setup thread rasterizes a direct triangle (direct.cuh): its samples lie in rows
+// [y0,y1) from column x0, up to column xend (exclusive); with exit_mask set, a row ends at
+// the first column where an edge in the mask (bit i: edge i, those with dy > 0) is negative.
+struct DirectWalk {
+    bool direct;
+    int xend;
+    uint32_t exit_mask;
+};
+
 // The record of one triangle with transformed vertices p1, p2, p3 (xyz) and face colour
-// c[0..2] in a w x h context.
+// c[0..2] in a w x h context.  With direct_max > 0, a triangle whose sample range holds at
+// most direct_max samples is marked for the direct path (dw): such a triangle needs no
+// proven tight bound nor depth bounds.  A finite triangle with an edge of dy > 0 is sized
+// by its unproven right end floor(max.x)+1 (xe) and walked with early row exits up to the
+// reference's bound; any other triangle is sized and walked by its stored range.  A
+// triangle is direct exactly when is_direct(x0, xe, y0, y1, direct_max) holds for the
+// stored range, so later kernels recognise it from row 4 alone.
 __device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p3, const uint8_t *c,
-                                                  int w, int h)
+                                                  int w, int h, int direct_max = 0, DirectWalk *dw = nullptr)
 {
     TriRecord r;
     r.v1x = p1.x; r.v1y = p1.y; r.v2x = p2.x; r.v2y = p2.y; r.v3x = p3.x; r.v3y = p3.y;
@@ -115,6 +131,7 @@ __device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p
     r.flags = finite ? kFlagFiniteXY : 0u;
     r.xe = x1;
     r.zlo = -INFINITY;
+    if (dw) *dw = DirectWalk{false, 0, 0u};
     if (finite && r.x0 < x1 && r.y0 < r.y1) {
         // back faces first: the bounds over the untightened range hold over any subrange,
         // so a triangle proven empty here needs no tighter range
@@ -122,6 +139,19 @@ __device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p
             r.xe = r.x0;
             r.flags |= kFlagCulled;
             return r;
+        }
+        if (direct_max > 0) {
+            // Along a row an edge of dy > 0 is non-increasing in x (monotone correctly
+            // rounded steps, finite values): once negative it stays negative, so a row walk
+            // may stop there.  floor(max.x)+1 only sizes the triangle.
+            const uint32_t mask = (r.dy0 > 0.0f ? 1u : 0u) | (r.dy1 > 0.0f ? 2u : 0u) | (r.dy2 > 0.0f ? 4u : 0u);
+            const float xf = fadd(floorf(mxx), 1.0f);
+            const int xa = xf <= (float)r.x0 ? r.x0 : (xf < (float)x1 ? (int)xf : x1);
+            if (mask && is_direct(r.x0, xa, r.y0, r.y1, direct_max)) {
+                r.xe = xa;
+                if (dw) *dw = DirectWalk{true, x1, mask};
+                return r;
+            }
         }
         // first column strictly right of the triangle, not left of x0
         const float xf = fadd(floorf(mxx), 1.0f);
@@ -144,6 +174,8 @@ __device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p
             }
         }
     }
+    // any other triangle with a range of at most direct_max samples is walked over it whole
+    if (dw && direct_max > 0 && is_direct(r.x0, r.xe, r.y0, r.y1, direct_max)) *dw = DirectWalk{true, r.xe, 0u};
     return r;
 }
 

@@ -60,17 +60,18 @@ __device__ __forceinline__ float4 transform_vertex(const MeshDev &mesh, const Ma
     return make_float4(row_dot(&M.m[0], x, y, z), row_dot(&M.m[4], x, y, z), row_dot(&M.m[8], x, y, z), 0.0f);
 }
 
-// tv null (soups): each thread transforms its triangle's three vertices itself, which
-// saves the vertex kernel and its round trip through memory.
-__global__ void __launch_bounds__(kMaxTrianglesPerBlock)
-setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_base, FrameGeom g,
-             FrameBuffers fb, BinBuffers bb)
+// One triangle of the draw (t >= mesh.ntri: none; every lane of the warp calls it for the
+// warp-wide steps): its record, its small-triangle tile counts or large-queue slot, and the
+// direct folds of the smallest triangles.
+__device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4 *__restrict__ tv, const Mat4 &M,
+                                               uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
+                                               const BinBuffers &bb, uint32_t t)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = t < mesh.ntri;
     bool large = false, direct = false;
     TriRecord r;
     TileSpan sp{};
+    DirectWalk dw{false, 0, 0u};
     const Viewport vp = to_vp(g);
     if (live) {
         uint32_t i1, i2, i3;
@@ -82,13 +83,14 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
             i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
         }
         if (tv)
-            r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), mesh.rgb + 3 * (size_t)t, g.w, g.h);
+            r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), mesh.rgb + 3 * (size_t)t, g.w, g.h,
+                             g.direct_max, &dw);
         else
             r = build_record(transform_vertex(mesh, M, i1), transform_vertex(mesh, M, i2),
-                             transform_vertex(mesh, M, i3), mesh.rgb + 3 * (size_t)t, g.w, g.h);
+                             transform_vertex(mesh, M, i3), mesh.rgb + 3 * (size_t)t, g.w, g.h, g.direct_max, &dw);
         sp = tile_span(vp, r);
         store_record(fb.records + tri_base + t, r, sp.ntiles);
-        direct = is_direct(r.x0, r.xe, r.y0, r.y1, g.direct_max);
+        direct = dw.direct;
         large = sp.large && !direct;
     }
     // binning: count tiles of small triangles here, queue the rest for warps
@@ -101,10 +103,22 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
     // the smallest triangles fold their samples into the global keys here (direct.cuh)
     if (__any_sync(0xffffffffu, direct)) {
         const uint32_t frags = direct ? direct_raster(r, tri_base + t, g.w, g.pitch,
-                                                      reinterpret_cast<unsigned long long *>(fb.keys))
+                                                      reinterpret_cast<unsigned long long *>(fb.keys), dw.xend,
+                                                      dw.exit_mask)
                                       : 0u;
         add_frags_warp(frags, fb.fragments);
     }
+}
+
+// tv null (soups): each thread transforms its triangle's three vertices itself, which
+// saves the vertex kernel and its round trip through memory.
+__global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks)
+setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_base, FrameGeom g,
+             FrameBuffers fb, BinBuffers bb, int tpb)
+{
+    for (uint32_t t = blockIdx.x * (uint32_t)tpb + threadIdx.x; t < (blockIdx.x + 1u) * (uint32_t)tpb;
+         t += blockDim.x)
+        setup_triangle(mesh, tv, M, tri_base, g, fb, bb, t);
 }
 
 // Newline sentinels (src/rasterizer.rs:89-91): in image mode every row y in [y0,y1) of
@@ -215,7 +229,8 @@ cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, u
 {
     if (mesh.ntri == 0) return cudaSuccess;
     if (!valid_triangles_per_block(tpb)) return cudaErrorInvalidValue;
-    setup_kernel<<<(mesh.ntri + tpb - 1) / tpb, tpb, 0, s>>>(mesh, tv, M, tri_base, g, fb, bb);
+    setup_kernel<<<(mesh.ntri + tpb - 1) / tpb, setup_block_threads(tpb), 0, s>>>(mesh, tv, M, tri_base, g, fb, bb,
+                                                                                   tpb);
     return cudaGetLastError();
 }
 

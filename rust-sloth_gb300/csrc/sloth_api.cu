@@ -980,7 +980,7 @@ sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value)
         return SLOTH_OK;
     case SLOTH_OPTION_TRIANGLES_PER_BLOCK:
         if (!valid_triangles_per_block(value))
-            return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "triangles per block %lld is not 128, 256 or 512",
+            return fail(ctx, SLOTH_ERR_INVALID_ARGUMENT, "triangles per block %lld is not 128, 256, 1024 or 4096",
                         (long long)value);
         ctx->tpb = (int)value;
         return SLOTH_OK;

@@ -95,12 +95,17 @@ struct Mat4 {
     float m[16];             // row-major
 };
 
-// Triangles per block of the setup and fill kernels (one thread per triangle): a tuning
-// choice, the results do not depend on it.
-constexpr int kDefaultTrianglesPerBlock = 256;
-constexpr int kMaxTrianglesPerBlock = 512;
-constexpr int kTrianglesPerBlockChoices[3] = {128, 256, 512};
-inline bool valid_triangles_per_block(long long v) { return v == 128 || v == 256 || v == 512; }
+// Triangles per block of the setup and fill kernels: a tuning choice, the results do not
+// depend on it.  A block has min(tpb, kSetupThreads) threads, and each thread takes
+// tpb / threads triangles in turn (consecutive threads, consecutive triangles), so that a
+// triangle's record stores and key reductions drain while the thread sets up the next.
+constexpr int kSetupThreads = 256;
+constexpr int kSetupMinBlocks = 3;   // resident setup blocks per SM the register budget keeps
+constexpr int kFillMinBlocks = 4;    // the same for the fill kernels
+constexpr int kDefaultTrianglesPerBlock = 1024;
+constexpr int kTrianglesPerBlockChoices[4] = {128, 256, 1024, 4096};
+inline bool valid_triangles_per_block(long long v) { return v == 128 || v == 256 || v == 1024 || v == 4096; }
+__host__ __device__ inline int setup_block_threads(int tpb) { return tpb < kSetupThreads ? tpb : kSetupThreads; }
 
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked
 // up once per device): grids of the grid-stride kernels are sized by it.

@@ -93,13 +93,13 @@ def test_batch_every_tile_shape_and_autotune(ctx):
         b.set_direct_samples(direct)
         b.render()
         check_frames(b, meshes, frames, f"direct {direct}")
-    for tpb in (128, 512):
+    for tpb in (128, 4096):
         b.set_triangles_per_block(tpb)
         b.render()
         check_frames(b, meshes, frames, f"{tpb} triangles per block")
     best = b.autotune(reps=2)
     assert 0 <= best["shape"] < len(S.tile_shapes()) and best["direct"] in (0, 4, 16, 64)
-    assert best["tpb"] in (128, 256, 512) and best["ms"] > 0
+    assert best["tpb"] in (128, 256, 1024, 4096) and best["ms"] > 0
     b.render()
     check_frames(b, meshes, frames, "autotuned")
     b.close()
@@ -126,7 +126,7 @@ def test_batch_entry_overflow_replans(ctx):
     b.close()
 
 
-@pytest.mark.parametrize("direct,tpb", [(0, 128), (16, 512), (4, 256)])
+@pytest.mark.parametrize("direct,tpb", [(0, 128), (16, 4096), (4, 256)])
 def test_context_tuning_settings(ctx, direct, tpb):
     """Every value of the autotuner's other dimensions renders the same frame."""
     m = W.soup(6000, seed=52, n_large=15)
@@ -140,7 +140,7 @@ def test_context_tuning_settings(ctx, direct, tpb):
             ref = oracle_render([m], R, w, h, image, U=U)
             assert_same(gpu_render(ctx, [m], R, w, h, image, U=U, depth_cull=True), ref, f"{direct}/{tpb} {w}x{h}")
     finally:
-        ctx.set_triangles_per_block(256)
+        ctx.set_triangles_per_block(1024)
         ctx.set_direct_samples(0)
 
 
@@ -153,14 +153,14 @@ def test_context_autotune_renders_the_same_frame(ctx):
     ctx.update([dm])
     best = ctx.autotune([(dm, R)], reps=2)
     assert 0 <= best["shape"] < len(S.tile_shapes()) and best["direct"] in (0, 4, 16, 64)
-    assert best["tpb"] in (128, 256, 512) and best["ms"] > 0
+    assert best["tpb"] in (128, 256, 1024, 4096) and best["ms"] > 0
     ctx.clear()
     ctx.draw_mesh(dm, R)
     cells, z, winner = ctx.read()
     assert_same((cells, z, winner, None), oracle_render([m], R, w, h, True), "autotuned context")
     ctx.set_tile_shape(0)
     ctx.set_direct_samples(0)
-    ctx.set_triangles_per_block(256)
+    ctx.set_triangles_per_block(1024)
 
 
 @pytest.mark.parametrize("shape", range(5))
