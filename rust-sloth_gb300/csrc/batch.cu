@@ -77,7 +77,17 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
         direct = dw.direct;
         large = sp.large && !direct;
     }
-    count_small_tiles_warp(live && !large && !direct, r, vp, sp, b.bb.tile_count + f.tile_off);
+    const bool binned = live && !large && !direct && sp.ntiles != 0;
+    count_small_tiles_warp(binned, r, vp, sp, b.bb.tile_count + f.tile_off);
+    // the fill's work list: one atomic per warp
+    const unsigned bm = __ballot_sync(0xffffffffu, binned);
+    if (bm) {
+        const int lane = threadIdx.x & 31;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(b.fill_count, (uint32_t)__popc(bm));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (binned) b.fill_list[base + __popc(bm & ((1u << lane) - 1u))] = make_uint2(d.frame, d.local_base + t);
+    }
     if (__any_sync(0xffffffffu, large)) {
         const int q = large_slot(large, sp.ntiles, b.bb.large_count, b.bb.large_cap);
         if (q >= 0) {
@@ -153,34 +163,26 @@ __global__ void __launch_bounds__(256) batch_bin_large_kernel(BatchDev b)
     }
 }
 
-// One triangle of draw d: a small triangle's tile entries.
-__device__ __forceinline__ void batch_fill_triangle(const BatchDev &b, const BatchDraw &d, uint32_t t)
+// The small binned triangles setup listed, 256 per block and round (grid-stride): their
+// tile entries.  A warp's lanes may hold triangles of different frames; their tiles are
+// global tile indices.
+__global__ void __launch_bounds__(kSetupThreads, kFillMinBlocks) batch_fill_kernel(BatchDev b)
 {
-    const BatchFrame &f = b.frames[d.frame];
-    const uint32_t gtri = d.local_base + t;
-    const Viewport vp = vp_batch(f.g);
-    const bool live = t < d.mesh.ntri;
-    TriRecord r;
-    TileSpan sp{};
-    if (live) {
-        // the sample range first: culled and off-screen triangles end here
-        const int4 xr = __ldg(reinterpret_cast<const int4 *>(f.fb.records + gtri) + 4);
-        if (xr.x < xr.y && xr.z < xr.w && !is_direct(xr.x, xr.y, xr.z, xr.w, f.g.direct_max)) {
-            r = f.fb.records[gtri];
+    const uint32_t n = *b.fill_count;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool live = i < n;
+        const uint2 e = live ? b.fill_list[i] : make_uint2(0u, 0u);
+        const BatchFrame &f = b.frames[e.x];
+        const Viewport vp = vp_batch(f.g);
+        TriRecord r;
+        TileSpan sp{};
+        if (live) {
+            r = load_record(f.fb.records, e.y);
             sp = tile_span(vp, r);
         }
+        fill_small_warp(live, r, e.y, vp, sp, b.bb.tile_cursor, b.bb.entries, b.bb.capacity, f.tile_off);
     }
-    fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, b.bb.tile_cursor + f.tile_off,
-                    b.bb.entries, b.bb.capacity);
-}
-
-// blocks[i] = (draw, first triangle): the setup kernel's partition.
-__global__ void __launch_bounds__(kSetupThreads, kFillMinBlocks) batch_fill_kernel(BatchDev b, const int2 *__restrict__ blocks)
-{
-    const int2 blk = blocks[blockIdx.x];
-    const BatchDraw &d = b.draws[blk.x];
-    for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < (uint32_t)blk.y + (uint32_t)b.tpb; t += blockDim.x)
-        batch_fill_triangle(b, d, t);
 }
 
 __device__ __forceinline__ uint32_t frame_of_tile(const BatchDev &b, uint32_t tile)
@@ -327,11 +329,9 @@ cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s)
+cudaError_t launch_batch_fill(const BatchDev &b, cudaStream_t s)
 {
-    if (!nblocks) return cudaSuccess;
-    if (!valid_triangles_per_block(b.tpb)) return cudaErrorInvalidValue;
-    batch_fill_kernel<<<nblocks, setup_block_threads(b.tpb), 0, s>>>(b, blocks);
+    batch_fill_kernel<<<kFillMinBlocks * 2 * device_sm_count(), kSetupThreads, 0, s>>>(b);
     return cudaGetLastError();
 }
 

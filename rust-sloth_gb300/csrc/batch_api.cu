@@ -64,6 +64,8 @@ struct sloth_batch {
     uint32_t *large_frame = nullptr;
     uint32_t *overflow = nullptr;
     uint32_t *queue = nullptr;                // the persistent raster's item counter
+    uint2 *fill_list = nullptr;               // the fill's work list (one entry per record at most)
+    uint32_t *fill_count = nullptr;
     uint32_t *h_total = nullptr;              // pinned
     uint32_t *h_overflow = nullptr;           // pinned
     uint32_t *error = nullptr;                // device error word of the raster (sticky)
@@ -159,6 +161,8 @@ void free_layout(sloth_batch *b)
     b->bb.item_capacity = 0;
     bfree(b->overflow);
     bfree(b->queue);
+    bfree(b->fill_list);
+    bfree(b->fill_count);
     for (auto &p : b->blk) bfree(p);
     b->entries_cap = 0;
     b->rendered = false;
@@ -280,6 +284,8 @@ sloth_status build(sloth_batch *b, int shape)
     BCU(b, balloc(&b->bb.slice_offset, tiles + 4));
     BCU(b, balloc(&b->overflow, 1));
     BCU(b, balloc(&b->queue, 1));
+    BCU(b, balloc(&b->fill_list, rec));
+    BCU(b, balloc(&b->fill_count, 1));
     BCU(b, balloc(&b->d_mats, nd));
     for (uint32_t f = 0; f < nf; ++f) {
         BatchFrame &bf = b->hframes[f];
@@ -326,6 +332,8 @@ BatchDev dev_view(sloth_batch *b)
     d.large_frame = b->large_frame;
     d.overflow = b->overflow;
     d.queue = b->queue;
+    d.fill_list = b->fill_list;
+    d.fill_count = b->fill_count;
     d.depth_cull = sloth_ctx_depth_cull(b->ctx);
     d.tpb = b->tpb;
     return d;
@@ -346,6 +354,7 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     }
     if ((e = cudaMemsetAsync(b->nltree, 0xff, (size_t)b->total_nl * 4, s))) return e;
     if ((e = cudaMemsetAsync(b->bb.large_count, 0, 8, s))) return e;
+    if ((e = cudaMemsetAsync(b->fill_count, 0, 4, s))) return e;
     if ((e = cudaMemsetAsync(b->fragments, 0, 8, s))) return e;
     if ((e = cudaMemsetAsync(b->overflow, 0, 4, s))) return e;
     if ((e = cudaMemcpyAsync(b->d_mats, b->h_mats, b->meshes.size() * sizeof(Mat4), cudaMemcpyHostToDevice, s)))
@@ -368,7 +377,7 @@ cudaError_t enqueue_back(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     if ((e = cudaStreamWaitEvent(b->aux_s, b->ev_fill, 0))) return e;
     if ((e = launch_batch_bin_large(d, true, b->aux_s))) return e;
     if ((e = cudaEventRecord(b->ev_aux, b->aux_s))) return e;
-    if ((e = launch_batch_fill(d, b->blk[1], b->nblk[1], s))) return e;
+    if ((e = launch_batch_fill(d, s))) return e;
     if ((e = cudaStreamWaitEvent(s, b->ev_aux, 0))) return e;
     if ((e = launch_batch_items(d, s))) return e;
     const int tw = kTileShapes[b->shape][0], th = kTileShapes[b->shape][1];

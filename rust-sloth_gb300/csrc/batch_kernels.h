@@ -46,6 +46,9 @@ struct BatchDev {
     uint32_t *large_frame;     // frame of each large-queue entry
     uint32_t *overflow;        // set when the entries outgrew their capacity
     uint32_t *queue;           // the persistent raster's next item (zeroed by the item kernel)
+    uint2 *fill_list;          // (frame, frame-local draw index) of every small binned triangle,
+                               // appended by setup: the fill walks only these
+    uint32_t *fill_count;      // entries of fill_list (zeroed at the start of a render)
     int depth_cull;
     int tpb;                   // triangles per setup/fill block (the triangle block table's step)
 };
@@ -56,7 +59,7 @@ cudaError_t launch_batch_setup(const BatchDev &b, const int2 *blocks, uint32_t n
 cudaError_t launch_batch_newline(const BatchDev &b, const int2 *blocks, uint32_t nblocks, int max_nl,
                                  cudaStream_t s);
 cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s);
-cudaError_t launch_batch_fill(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s);
+cudaError_t launch_batch_fill(const BatchDev &b, cudaStream_t s);
 cudaError_t launch_batch_items(const BatchDev &b, cudaStream_t s);
 cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, bool persistent, cudaStream_t s);
 cudaError_t launch_batch_resolve(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s);

@@ -120,17 +120,18 @@ __device__ __forceinline__ void bin_large_warp(const TriRecord *rec, uint32_t gt
 
 // Writes a small triangle's entries.  Called by all 32 lanes (lanes with active false
 // write nothing); each lane's first tile takes its slots with one atomic per distinct
-// tile of the warp, like count_small_tiles_warp.
+// tile of the warp, like count_small_tiles_warp.  A lane's tiles are tile_base + the
+// frame-local index in tile_cursor (lanes of one warp may belong to different frames).
 __device__ __forceinline__ void fill_small_warp(bool active, const TriRecord &r, uint32_t gtri, const Viewport &vp,
                                                 const TileSpan &sp, uint32_t *tile_cursor, uint64_t *entries,
-                                                uint32_t capacity)
+                                                uint32_t capacity, uint32_t tile_base = 0)
 {
     uint32_t first = 0xffffffffu;
     bool first_wrapped = false;
     if (active) {
         auto put = [&](int tr, int tc) {
             const bool wrapped = !sp.W.empty() && !clip_wrapped(vp, sp.W, tr, tc).empty();
-            const uint32_t tile = tr * vp.ntx + tc;
+            const uint32_t tile = tile_base + tr * vp.ntx + tc;
             if (first == 0xffffffffu) {
                 first = tile;
                 first_wrapped = wrapped;
