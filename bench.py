@@ -298,10 +298,17 @@ def run_gpu(args):
     R = S.euler_rotation(*W.cli_rotation())
 
     ctx = S.Context(local, stream=stream.cuda_stream)
-    ctx.set_direct_samples(args.direct)
     dm = S.Mesh(ctx, m["x"], m["y"], m["z"], m["rgb"])
     ctx.set_viewport(W_PX, H_PX, True)
     ctx.update([dm])
+    if args.direct >= 0:
+        tuned = {"shape": 0, "direct": args.direct, "tpb": 256, "autotuned": False}
+    else:
+        # the autotuner picks (tile shape, direct limit, triangles per block) on this frame
+        tuned = {**ctx.autotune([(dm, R)], reps=3), "autotuned": True}
+    ctx.set_tile_shape(tuned["shape"])
+    ctx.set_direct_samples(tuned["direct"])
+    ctx.set_triangles_per_block(tuned["tpb"])
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def step():
@@ -399,7 +406,9 @@ def run_gpu(args):
         extra = []
         for _ in range(args.e2e_contexts - 1):
             c2 = S.Context(local)
-            c2.set_direct_samples(args.direct)
+            c2.set_tile_shape(tuned["shape"])
+            c2.set_direct_samples(tuned["direct"])
+            c2.set_triangles_per_block(tuned["tpb"])
             c2.set_viewport(W_PX, H_PX, True)
             d2 = S.Mesh(c2, m["x"], m["y"], m["z"], m["rgb"])
             c2.update([d2])
@@ -514,7 +523,9 @@ def run_gpu(args):
                    "l2": "flushed before every timed step (512 MiB write)", "parallelism": f"replicas x{ws}"},
         "gfrag_per_s": frags * value / 1e9, "fragments_per_frame": frags,
         "fragments_rasterized_per_frame": frags_evaluated,
-        "depth_cull": not args.no_depth_cull, "direct_samples": args.direct,
+        "depth_cull": not args.no_depth_cull,
+        "tuning": {"tile_shape": S.tile_shapes()[tuned["shape"]], "direct_samples": tuned["direct"],
+                   "triangles_per_block": tuned["tpb"], "autotuned": tuned["autotuned"]},
         "e2e": e2e,
         "gpu_launches": launches, "kernels": kernels, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
         "batched": batched, "differentiable": differentiable, "inverse_rendering": inverse,
@@ -599,7 +610,7 @@ def run_config3(torch, stream, device, args):
         forms[persistent] = time_batched()
     batched_ms = forms[tuned["persistent"]]
 
-    plain = {}
+    plain, plain_tuning = {}, {}
     if args.no_plain:
         plain_ms = float("nan")
     def plain_pass():
@@ -607,12 +618,11 @@ def run_config3(torch, stream, device, args):
             key = (f["w"], f["h"], f["image"])
             c = plain.get(key)
             if c is None:
-                # the same kernels and settings as the batch: only the launch structure differs
+                # one context per viewport size, autotuned for itself on its first frame
                 c = plain[key] = S.Context(device, stream=stream.cuda_stream)
-                c.set_tile_shape(shape)
-                c.set_direct_samples(direct)
-                c.set_triangles_per_block(tpb)
                 c.set_viewport(f["w"], f["h"], f["image"])
+                c.set_utransform(f["U"])
+                plain_tuning[key] = c.autotune(f["draws"], reps=2)
             c.set_utransform(f["U"])
             c.clear()
             for m, R in f["draws"]:
@@ -644,6 +654,8 @@ def run_config3(torch, stream, device, args):
            "raster": ("persistent: SMs x resident CTAs over the device item queue" if tuned["persistent"]
                       else "one CTA per item"),
            "persistent_ms_per_pass": forms[True], "one_cta_per_item_ms_per_pass": forms[False],
+           "plain_tuning": {f"{k[0]}x{k[1]}": {"tile_shape": S.tile_shapes()[v["shape"]], "direct_samples": v["direct"],
+                                               "triangles_per_block": v["tpb"]} for k, v in plain_tuning.items()},
            "autotuned": args.batched_shape < 0, "graph": True}
     if par is not None:
         out["bitexact_frames_vs_oracle"] = par["frames_bitexact"]
@@ -850,8 +862,9 @@ def main():
                     help="also time one whole config-2 frame on one thread (about a minute) beside the sample")
     ap.add_argument("--no-depth-cull", action="store_true",
                     help="rasterize every triangle (SLOTH_OPTION_DEPTH_CULL 0)")
-    ap.add_argument("--direct", type=int, default=0,
-                    help="SLOTH_OPTION_DIRECT_SAMPLES of the config-2 contexts (0: every triangle binned)")
+    ap.add_argument("--direct", type=int, default=-1,
+                    help="SLOTH_OPTION_DIRECT_SAMPLES of the config-2 contexts with the default tile shape and "
+                         "256 triangles per block (default: all three autotuned on the frame)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) leg")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the full-size checks against the oracle (config 2 frame, every config-3 frame)")

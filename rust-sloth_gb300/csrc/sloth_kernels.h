@@ -102,7 +102,7 @@ struct Mat4 {
 constexpr int kSetupThreads = 256;
 constexpr int kSetupMinBlocks = 3;   // resident setup blocks per SM the register budget keeps
 constexpr int kFillMinBlocks = 4;    // the same for the fill kernels
-constexpr int kDefaultTrianglesPerBlock = 1024;
+constexpr int kDefaultTrianglesPerBlock = 256;
 constexpr int kTrianglesPerBlockChoices[4] = {128, 256, 1024, 4096};
 inline bool valid_triangles_per_block(long long v) { return v == 128 || v == 256 || v == 1024 || v == 4096; }
 __host__ __device__ inline int setup_block_threads(int tpb) { return tpb < kSetupThreads ? tpb : kSetupThreads; }

@@ -140,7 +140,7 @@ def test_context_tuning_settings(ctx, direct, tpb):
             ref = oracle_render([m], R, w, h, image, U=U)
             assert_same(gpu_render(ctx, [m], R, w, h, image, U=U, depth_cull=True), ref, f"{direct}/{tpb} {w}x{h}")
     finally:
-        ctx.set_triangles_per_block(1024)
+        ctx.set_triangles_per_block(256)
         ctx.set_direct_samples(0)
 
 
@@ -160,7 +160,7 @@ def test_context_autotune_renders_the_same_frame(ctx):
     assert_same((cells, z, winner, None), oracle_render([m], R, w, h, True), "autotuned context")
     ctx.set_tile_shape(0)
     ctx.set_direct_samples(0)
-    ctx.set_triangles_per_block(1024)
+    ctx.set_triangles_per_block(256)
 
 
 @pytest.mark.parametrize("shape", range(5))
