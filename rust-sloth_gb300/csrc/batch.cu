@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(256) batch_vertex_kernel(BatchDev b, const int
 
 // One triangle of draw d (every lane of the warp calls it: t >= ntri is none): record,
 // small-triangle tile counts, large queue, and the direct folds of the smallest triangles.
+template <bool kDirect>
 __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const BatchDraw &d, uint32_t t)
 {
     const BatchFrame &f = b.frames[d.frame];
@@ -71,7 +72,7 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
         }
         const float4 *tv = b.tv + d.vert_off;
         r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), d.mesh.rgb + 3 * (size_t)t, f.g.w,
-                         f.g.h, f.g.direct_max, &dw);
+                         f.g.h, kDirect ? f.g.direct_max : 0, kDirect ? &dw : nullptr);
         sp = tile_span(vp, r);
         store_record(f.fb.records + d.local_base + t, r, sp.ntiles);
         direct = dw.direct;
@@ -96,7 +97,7 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
         }
     }
     // the smallest triangles fold their samples into the frame's global keys (direct.cuh)
-    if (__any_sync(0xffffffffu, direct)) {
+    if (kDirect && __any_sync(0xffffffffu, direct)) {
         const uint32_t frags = direct ? direct_raster(r, d.local_base + t, f.g.w, f.g.pitch,
                                                       reinterpret_cast<unsigned long long *>(f.fb.keys), dw.xend,
                                                       dw.exit_mask)
@@ -107,12 +108,13 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
 
 // blocks[i] = (draw, first triangle): b.tpb triangles of the draw, each thread taking
 // b.tpb / blockDim.x of them in turn.
-__global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
+template <bool kDirect>
+__global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFillMinBlocks) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
 {
     const int2 blk = blocks[blockIdx.x];
     const BatchDraw &d = b.draws[blk.x];
     for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < (uint32_t)blk.y + (uint32_t)b.tpb; t += blockDim.x)
-        batch_setup_triangle(b, d, t);
+        batch_setup_triangle<kDirect>(b, d, t);
 }
 
 // blocks[i] = (draw, first triangle of a chunk): newline segment tree of the draw's frame.
@@ -307,7 +309,8 @@ cudaError_t launch_batch_setup(const BatchDev &b, const int2 *blocks, uint32_t n
 {
     if (!nblocks) return cudaSuccess;
     if (!valid_triangles_per_block(b.tpb)) return cudaErrorInvalidValue;
-    batch_setup_kernel<<<nblocks, setup_block_threads(b.tpb), 0, s>>>(b, blocks);
+    if (b.direct_max > 0) batch_setup_kernel<true><<<nblocks, setup_block_threads(b.tpb), 0, s>>>(b, blocks);
+    else batch_setup_kernel<false><<<nblocks, setup_block_threads(b.tpb), 0, s>>>(b, blocks);
     return cudaGetLastError();
 }
 

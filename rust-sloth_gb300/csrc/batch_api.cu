@@ -336,6 +336,7 @@ BatchDev dev_view(sloth_batch *b)
     d.fill_count = b->fill_count;
     d.depth_cull = sloth_ctx_depth_cull(b->ctx);
     d.tpb = b->tpb;
+    d.direct_max = b->direct_max;
     return d;
 }
 

@@ -51,6 +51,7 @@ struct BatchDev {
     uint32_t *fill_count;      // entries of fill_list (zeroed at the start of a render)
     int depth_cull;
     int tpb;                   // triangles per setup/fill block (the triangle block table's step)
+    int direct_max;            // the frames' FrameGeom::direct_max (the same for every frame)
 };
 
 // Block tables: one int2 (item, start) per block, built on the host.

@@ -63,6 +63,7 @@ __device__ __forceinline__ float4 transform_vertex(const MeshDev &mesh, const Ma
 // One triangle of the draw (t >= mesh.ntri: none; every lane of the warp calls it for the
 // warp-wide steps): its record, its small-triangle tile counts or large-queue slot, and the
 // direct folds of the smallest triangles.
+template <bool kDirect>
 __device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4 *__restrict__ tv, const Mat4 &M,
                                                uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
                                                const BinBuffers &bb, uint32_t t)
@@ -82,12 +83,14 @@ __device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4
         } else {
             i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
         }
+        const int dmax = kDirect ? g.direct_max : 0;
+        DirectWalk *dwp = kDirect ? &dw : nullptr;
         if (tv)
             r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), mesh.rgb + 3 * (size_t)t, g.w, g.h,
-                             g.direct_max, &dw);
+                             dmax, dwp);
         else
             r = build_record(transform_vertex(mesh, M, i1), transform_vertex(mesh, M, i2),
-                             transform_vertex(mesh, M, i3), mesh.rgb + 3 * (size_t)t, g.w, g.h, g.direct_max, &dw);
+                             transform_vertex(mesh, M, i3), mesh.rgb + 3 * (size_t)t, g.w, g.h, dmax, dwp);
         sp = tile_span(vp, r);
         store_record(fb.records + tri_base + t, r, sp.ntiles);
         direct = dw.direct;
@@ -101,7 +104,7 @@ __device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4
         if (q >= 0) bb.large_queue[q] = t;
     }
     // the smallest triangles fold their samples into the global keys here (direct.cuh)
-    if (__any_sync(0xffffffffu, direct)) {
+    if (kDirect && __any_sync(0xffffffffu, direct)) {
         const uint32_t frags = direct ? direct_raster(r, tri_base + t, g.w, g.pitch,
                                                       reinterpret_cast<unsigned long long *>(fb.keys), dw.xend,
                                                       dw.exit_mask)
@@ -112,13 +115,15 @@ __device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4
 
 // tv null (soups): each thread transforms its triangle's three vertices itself, which
 // saves the vertex kernel and its round trip through memory.
-__global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks)
+// kDirect: compiled with the direct path (g.direct_max > 0), which needs more registers.
+template <bool kDirect>
+__global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFillMinBlocks)
 setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_base, FrameGeom g,
              FrameBuffers fb, BinBuffers bb, int tpb)
 {
     for (uint32_t t = blockIdx.x * (uint32_t)tpb + threadIdx.x; t < (blockIdx.x + 1u) * (uint32_t)tpb;
          t += blockDim.x)
-        setup_triangle(mesh, tv, M, tri_base, g, fb, bb, t);
+        setup_triangle<kDirect>(mesh, tv, M, tri_base, g, fb, bb, t);
 }
 
 // Newline sentinels (src/rasterizer.rs:89-91): in image mode every row y in [y0,y1) of
@@ -229,8 +234,11 @@ cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, u
 {
     if (mesh.ntri == 0) return cudaSuccess;
     if (!valid_triangles_per_block(tpb)) return cudaErrorInvalidValue;
-    setup_kernel<<<(mesh.ntri + tpb - 1) / tpb, setup_block_threads(tpb), 0, s>>>(mesh, tv, M, tri_base, g, fb, bb,
-                                                                                   tpb);
+    const uint32_t blocks = (mesh.ntri + tpb - 1) / tpb;
+    if (g.direct_max > 0)
+        setup_kernel<true><<<blocks, setup_block_threads(tpb), 0, s>>>(mesh, tv, M, tri_base, g, fb, bb, tpb);
+    else
+        setup_kernel<false><<<blocks, setup_block_threads(tpb), 0, s>>>(mesh, tv, M, tri_base, g, fb, bb, tpb);
     return cudaGetLastError();
 }
 

@@ -100,8 +100,8 @@ struct Mat4 {
 // tpb / threads triangles in turn (consecutive threads, consecutive triangles), so that a
 // triangle's record stores and key reductions drain while the thread sets up the next.
 constexpr int kSetupThreads = 256;
-constexpr int kSetupMinBlocks = 3;   // resident setup blocks per SM the register budget keeps
-constexpr int kFillMinBlocks = 4;    // the same for the fill kernels
+constexpr int kSetupMinBlocks = 3;   // resident setup blocks per SM the register budget keeps (direct path)
+constexpr int kFillMinBlocks = 4;    // the same for the fill kernels and setup without the direct path
 constexpr int kDefaultTrianglesPerBlock = 256;
 constexpr int kTrianglesPerBlockChoices[4] = {128, 256, 1024, 4096};
 inline bool valid_triangles_per_block(long long v) { return v == 128 || v == 256 || v == 1024 || v == 4096; }
