@@ -51,6 +51,24 @@ __global__ void __launch_bounds__(256) batch_vertex_kernel(BatchDev b, const int
 
 // One triangle of draw d (every lane of the warp calls it: t >= ntri is none): record,
 // small-triangle tile counts, large queue, and the direct folds of the smallest triangles.
+// The three transformed vertices of triangle t of draw d (the vertex kernel's output).
+__device__ __forceinline__ void batch_triangle_vertices(const BatchDev &b, const BatchDraw &d, uint32_t t, float4 &p1,
+                                                        float4 &p2, float4 &p3)
+{
+    uint32_t i1, i2, i3;
+    if (d.mesh.idx) {
+        i1 = __ldg(d.mesh.idx + 3 * (size_t)t + 0);
+        i2 = __ldg(d.mesh.idx + 3 * (size_t)t + 1);
+        i3 = __ldg(d.mesh.idx + 3 * (size_t)t + 2);
+    } else {
+        i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
+    }
+    const float4 *tv = b.tv + d.vert_off;
+    p1 = __ldg(tv + i1);
+    p2 = __ldg(tv + i2);
+    p3 = __ldg(tv + i3);
+}
+
 template <bool kDirect>
 __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const BatchDraw &d, uint32_t t)
 {
@@ -62,17 +80,10 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
     TileSpan sp{};
     const Viewport vp = vp_batch(f.g);
     if (live) {
-        uint32_t i1, i2, i3;
-        if (d.mesh.idx) {
-            i1 = __ldg(d.mesh.idx + 3 * (size_t)t + 0);
-            i2 = __ldg(d.mesh.idx + 3 * (size_t)t + 1);
-            i3 = __ldg(d.mesh.idx + 3 * (size_t)t + 2);
-        } else {
-            i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
-        }
-        const float4 *tv = b.tv + d.vert_off;
-        r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), d.mesh.rgb + 3 * (size_t)t, f.g.w,
-                         f.g.h, kDirect ? f.g.direct_max : 0, kDirect ? &dw : nullptr);
+        float4 p1, p2, p3;
+        batch_triangle_vertices(b, d, t, p1, p2, p3);
+        r = build_record(p1, p2, p3, d.mesh.rgb + 3 * (size_t)t, f.g.w, f.g.h, kDirect ? f.g.direct_max : 0,
+                         kDirect ? &dw : nullptr);
         sp = tile_span(vp, r);
         store_record(f.fb.records + d.local_base + t, r, sp.ntiles);
         direct = dw.direct;
@@ -108,13 +119,37 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
 
 // blocks[i] = (draw, first triangle): b.tpb triangles of the draw, each thread taking
 // b.tpb / blockDim.x of them in turn.
+
+// blocks[i] = (draw, first triangle): b.tpb triangles of the draw in the single-frame
+// setup's two phases (setup.cu): the range and the back-face proof for every triangle, the
+// rest of the setup for the ones queued in shared memory.
 template <bool kDirect>
 __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFillMinBlocks) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
 {
+    __shared__ uint32_t squeue[kMaxTrianglesPerBlock];
+    __shared__ uint32_t sq_n;
+    if (threadIdx.x == 0) sq_n = 0;
+    block_sync();
     const int2 blk = blocks[blockIdx.x];
     const BatchDraw &d = b.draws[blk.x];
-    for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < (uint32_t)blk.y + (uint32_t)b.tpb; t += blockDim.x)
-        batch_setup_triangle<kDirect>(b, d, t);
+    const BatchFrame &f = b.frames[d.frame];
+    for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < (uint32_t)blk.y + (uint32_t)b.tpb; t += blockDim.x) {
+        bool keep = false;
+        if (t < d.mesh.ntri) {
+            float4 p1, p2, p3;
+            batch_triangle_vertices(b, d, t, p1, p2, p3);
+            int4 row4;
+            keep = needs_setup(p1, p2, p3, f.g.w, f.g.h, row4);
+            if (!keep) reinterpret_cast<int4 *>(f.fb.records + d.local_base + t)[4] = row4;
+        }
+        queue_push(keep, t, squeue, &sq_n);
+    }
+    block_sync();
+    const uint32_t nq = sq_n;
+    for (uint32_t base = 0; base < nq; base += blockDim.x) {
+        const uint32_t q = base + threadIdx.x;
+        batch_setup_triangle<kDirect>(b, d, q < nq ? squeue[q] : 0xffffffffu);
+    }
 }
 
 // blocks[i] = (draw, first triangle of a chunk): newline segment tree of the draw's frame.
@@ -210,7 +245,7 @@ __global__ void __launch_bounds__(256) batch_items_kernel(BatchDev b)
     const SplitParams sp{b.bb.slice_offset[nt + 1], b.bb.slice_offset[nt + 2]};
     const uint32_t cnt = b.bb.tile_count[t], ns = tile_slices(cnt, sp);
     const bool split = cnt > sp.threshold;
-    const uint32_t off = b.bb.slice_offset[t] + (split ? 0u : b.bb.slice_offset[nt + 3]);
+    const uint32_t off = item_offset(b.bb.slice_offset, nt, t, cnt, sp.threshold);
     for (uint32_t k = 0; k < ns && off + k < b.bb.item_capacity; ++k) b.bb.items[off + k] = make_uint2(t, k);
     if (split) {
         const BatchFrame &f = b.frames[frame_of_tile(b, t)];

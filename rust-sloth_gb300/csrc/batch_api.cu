@@ -281,7 +281,7 @@ sloth_status build(sloth_batch *b, int shape)
     BCU(b, balloc(&b->bb.large_count, 2));
     b->bb.large_cap = (uint32_t)rec;
     BCU(b, balloc(&b->large_frame, rec));
-    BCU(b, balloc(&b->bb.slice_offset, tiles + 4));
+    BCU(b, balloc(&b->bb.slice_offset, tiles + kSliceExtra));
     BCU(b, balloc(&b->overflow, 1));
     BCU(b, balloc(&b->queue, 1));
     BCU(b, balloc(&b->fill_list, rec));

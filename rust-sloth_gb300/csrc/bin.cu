@@ -41,16 +41,21 @@ __device__ __forceinline__ SplitParams split_params(const BinBuffers &bb, uint32
 
 // Exclusive scans of the tile entry counts (offsets, cursors; offsets[n] = total) and of
 // the raster items per tile, by one block, 4096 tiles per step with running carries.  A
-// first pass sets the split threshold from the mean entries of a non-empty tile; the
-// items of split tiles are numbered first (slice_offset counts them apart; the item
-// kernel adds the split tiles' item count to the others').
+// first pass sets the split threshold and the light threshold from the mean entries of a
+// non-empty tile.  Items are numbered in three classes: split tiles' slices first (they
+// start first), then the other tiles in tile order, then light tiles (fewer entries than
+// a quarter of the mean: mostly the frame's nearly empty borders) last, so that the last
+// wave of a launch is made of short CTAs.  slice_offset[t] is the tile's first item within
+// its class; item_offset() adds the class base.
 __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers bb)
 {
+    constexpr int kV = 4;   // running sums: entries, split items, other items, light items
     __shared__ unsigned long long red_e[32];
     __shared__ uint32_t red_t[32];
-    __shared__ uint32_t ws_e[32], ws_h[32], ws_l[32];
-    __shared__ uint32_t carry_e, carry_h, carry_l;
+    __shared__ uint32_t ws[kV][32];
+    __shared__ uint32_t carry[kV];
     __shared__ SplitParams sp_s;
+    __shared__ uint32_t light_s;
     const uint32_t tid = threadIdx.x;
     const int lane = tid & 31, wid = tid >> 5;
     // pass 1: entries and non-empty tiles
@@ -70,7 +75,7 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
         red_e[wid] = se;
         red_t[wid] = st;
     }
-    if (tid == 0) carry_e = carry_h = carry_l = 0;
+    if (tid < kV) carry[tid] = 0;
     block_sync();
     if (tid == 0) {
         unsigned long long te = 0;
@@ -86,86 +91,81 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
         if (thr < kMinSplitEntries) thr = kMinSplitEntries;
         sp_s.threshold = (uint32_t)(thr < 0x40000000ull ? thr : 0x40000000ull);
         sp_s.slice = sp_s.threshold / 2;
+        light_s = (uint32_t)(mean / 4 < sp_s.threshold ? mean / 4 : sp_s.threshold);
     }
     block_sync();
     const SplitParams sp = sp_s;
+    const uint32_t light = light_s;
     // pass 2: the scans
     for (uint32_t base = 0; base < n; base += 4 * 1024) {
         const uint32_t i0 = base + 4 * tid;
-        uint32_t c[4], hs[4], ls[4], le = 0, lh = 0, ll = 0;
+        uint32_t c[4], cls[4], loc[kV] = {0, 0, 0, 0};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             c[k] = i0 + k < n ? bb.tile_count[i0 + k] : 0u;
-            const uint32_t ns = tile_slices(c[k], sp);
-            hs[k] = c[k] > sp.threshold ? ns : 0u;
-            ls[k] = c[k] > sp.threshold ? 0u : ns;
-            le += c[k];
-            lh += hs[k];
-            ll += ls[k];
+            cls[k] = c[k] > sp.threshold ? 1u : (c[k] < light ? 3u : 2u);
+            loc[0] += c[k];
+            loc[cls[k]] += tile_slices(c[k], sp);
         }
-        uint32_t ve = le, vh = lh, vl = ll;
+        uint32_t v[kV];
+#pragma unroll
+        for (int q = 0; q < kV; ++q) v[q] = loc[q];
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t oe = __shfl_up_sync(0xffffffffu, ve, d), oh = __shfl_up_sync(0xffffffffu, vh, d),
-                           ol = __shfl_up_sync(0xffffffffu, vl, d);
-            if (lane >= d) {
-                ve += oe;
-                vh += oh;
-                vl += ol;
+#pragma unroll
+            for (int q = 0; q < kV; ++q) {
+                const uint32_t o = __shfl_up_sync(0xffffffffu, v[q], d);
+                if (lane >= d) v[q] += o;
             }
         }
-        if (lane == 31) {
-            ws_e[wid] = ve;
-            ws_h[wid] = vh;
-            ws_l[wid] = vl;
-        }
+        if (lane == 31)
+#pragma unroll
+            for (int q = 0; q < kV; ++q) ws[q][wid] = v[q];
         block_sync();
         if (wid == 0) {
-            uint32_t a = ws_e[lane], b = ws_h[lane], d3 = ws_l[lane];
+            uint32_t a[kV];
+#pragma unroll
+            for (int q = 0; q < kV; ++q) a[q] = ws[q][lane];
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t oa = __shfl_up_sync(0xffffffffu, a, d), ob = __shfl_up_sync(0xffffffffu, b, d),
-                               oc = __shfl_up_sync(0xffffffffu, d3, d);
-                if (lane >= d) {
-                    a += oa;
-                    b += ob;
-                    d3 += oc;
+#pragma unroll
+                for (int q = 0; q < kV; ++q) {
+                    const uint32_t o = __shfl_up_sync(0xffffffffu, a[q], d);
+                    if (lane >= d) a[q] += o;
                 }
             }
-            ws_e[lane] = a;
-            ws_h[lane] = b;
-            ws_l[lane] = d3;
+#pragma unroll
+            for (int q = 0; q < kV; ++q) ws[q][lane] = a[q];
         }
         block_sync();
-        uint32_t pe = carry_e + ve - le + (wid > 0 ? ws_e[wid - 1] : 0u);
-        uint32_t ph = carry_h + vh - lh + (wid > 0 ? ws_h[wid - 1] : 0u);
-        uint32_t pl = carry_l + vl - ll + (wid > 0 ? ws_l[wid - 1] : 0u);
+        uint32_t p[kV];
+#pragma unroll
+        for (int q = 0; q < kV; ++q) p[q] = carry[q] + v[q] - loc[q] + (wid > 0 ? ws[q][wid - 1] : 0u);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             if (i0 + k < n) {
-                bb.tile_offset[i0 + k] = pe;
-                bb.tile_cursor[i0 + k] = pe;
-                bb.slice_offset[i0 + k] = c[k] > sp.threshold ? ph : pl;
+                bb.tile_offset[i0 + k] = p[0];
+                bb.tile_cursor[i0 + k] = p[0];
+                bb.slice_offset[i0 + k] = p[cls[k]];
             }
-            pe += c[k];
-            ph += hs[k];
-            pl += ls[k];
+            p[0] += c[k];
+            p[cls[k]] += tile_slices(c[k], sp);
         }
         block_sync();                    // every thread has read the carries
-        if (tid == blockDim.x - 1) {
-            carry_e = pe;
-            carry_h = ph;
-            carry_l = pl;
-        }
+        if (tid == blockDim.x - 1)
+#pragma unroll
+            for (int q = 0; q < kV; ++q) carry[q] = p[q];
         block_sync();
     }
     if (tid == 0) {
-        if (bb.max_total) atomicMax(bb.max_total, carry_e);
-        bb.tile_offset[n] = carry_e;
-        bb.slice_offset[n] = carry_h + carry_l;
+        if (bb.max_total) atomicMax(bb.max_total, carry[0]);
+        bb.tile_offset[n] = carry[0];
+        bb.slice_offset[n] = carry[1] + carry[2] + carry[3];
         bb.slice_offset[n + 1] = sp.threshold;
         bb.slice_offset[n + 2] = sp.slice;
-        bb.slice_offset[n + 3] = carry_h;
+        bb.slice_offset[n + 3] = carry[1];
+        bb.slice_offset[n + 4] = carry[1] + carry[2];
+        bb.slice_offset[n + 5] = light;
     }
 }
 
@@ -193,7 +193,7 @@ bin_items_kernel(uint32_t n, FrameGeom g, FrameBuffers fb, BinBuffers bb)
     const SplitParams sp = split_params(bb, n);
     const uint32_t cnt = bb.tile_count[t], ns = tile_slices(cnt, sp);
     const bool split = cnt > sp.threshold;
-    const uint32_t off = bb.slice_offset[t] + (split ? 0u : bb.slice_offset[n + 3]);
+    const uint32_t off = item_offset(bb.slice_offset, n, t, cnt, sp.threshold);
     for (uint32_t k = 0; k < ns && off + k < bb.item_capacity; ++k) bb.items[off + k] = make_uint2(t, k);
     if (split && fb.tile_gen[t] != fb.gen) {
         const int tr = (int)t / g.ntx, tc = (int)t - tr * g.ntx;

@@ -79,6 +79,39 @@ __device__ __forceinline__ void store_record(TriRecord *dst, const TriRecord &r,
     else reinterpret_cast<int4 *>(dst)[4] = make_int4(r.x0, r.xe, r.y0, r.y1);
 }
 
+// The first steps of build_record, for a setup kernel that sets triangles aside before the
+// rest of their setup: the sample range and the back-face proof over the untightened range
+// (the same operations as build_record).  Returns false for a triangle with an empty range
+// or proven to cover no sample, with `row4` its record row 4 (x0, xe, y0, y1) -- all that
+// is ever read of such a triangle; true when the triangle needs build_record.
+__device__ __forceinline__ bool needs_setup(float4 p1, float4 p2, float4 p3, int w, int h, int4 &row4)
+{
+    TriRecord r;   // the fields orient_bound reads
+    r.v1x = p1.x; r.v1y = p1.y; r.v2x = p2.x; r.v2y = p2.y; r.v3x = p3.x; r.v3y = p3.y;
+    r.dx0 = fsub(p3.x, p2.x); r.dy0 = fsub(p3.y, p2.y);
+    r.dx1 = fsub(p1.x, p3.x); r.dy1 = fsub(p1.y, p3.y);
+    r.dx2 = fsub(p2.x, p1.x); r.dy2 = fsub(p2.y, p1.y);
+    const float mnx = fminf(p1.x, fminf(p2.x, p3.x)), mny = fminf(p1.y, fminf(p2.y, p3.y));
+    const float mxx = fmaxf(p1.x, fmaxf(p2.x, p3.x)), mxy = fmaxf(p1.y, fmaxf(p2.y, p3.y));
+    r.x0 = sat_lo(ceilf(fmaxf(mnx, 1.0f)), w);
+    r.y0 = sat_lo(ceilf(fmaxf(mny, 1.0f)), h);
+    const int x1 = sat_hi(ceilf(fminf(fmul(mxx, 2.0f), (float)(w - 1))));
+    r.y1 = sat_hi(ceilf(fminf(mxy, (float)(h - 1))));
+    r.xe = x1;
+    if (!(r.x0 < x1 && r.y0 < r.y1)) {
+        row4 = make_int4(r.x0, x1, r.y0, r.y1);
+        return false;
+    }
+    const float big = 1e18f;
+    const bool finite = fabsf(p1.x) < big && fabsf(p1.y) < big && fabsf(p2.x) < big &&
+                        fabsf(p2.y) < big && fabsf(p3.x) < big && fabsf(p3.y) < big;
+    if (finite && provably_empty(orient_bound(r))) {
+        row4 = make_int4(r.x0, r.x0, r.y0, r.y1);
+        return false;
+    }
+    return true;
+}
+
 // How the setup thread rasterizes a direct triangle (direct.cuh): its samples lie in rows
 // [y0,y1) from column x0, up to column xend (exclusive); with exit_mask set, a row ends at
 // the first column where an edge in the mask (bit i: edge i, those with dy > 0) is negative.

@@ -60,6 +60,26 @@ __device__ __forceinline__ float4 transform_vertex(const MeshDev &mesh, const Ma
     return make_float4(row_dot(&M.m[0], x, y, z), row_dot(&M.m[4], x, y, z), row_dot(&M.m[8], x, y, z), 0.0f);
 }
 
+// The three transformed vertices of triangle t.  tv null (soups): the thread transforms
+// them itself, which saves the vertex kernel and its round trip through memory.
+__device__ __forceinline__ void triangle_vertices(const MeshDev &mesh, const float4 *__restrict__ tv, const Mat4 &M,
+                                                  uint32_t t, float4 &p1, float4 &p2, float4 &p3)
+{
+    uint32_t i1, i2, i3;
+    if (mesh.idx) {
+        i1 = __ldg(mesh.idx + 3 * (size_t)t + 0);
+        i2 = __ldg(mesh.idx + 3 * (size_t)t + 1);
+        i3 = __ldg(mesh.idx + 3 * (size_t)t + 2);
+    } else {
+        i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
+    }
+    if (tv) {
+        p1 = __ldg(tv + i1); p2 = __ldg(tv + i2); p3 = __ldg(tv + i3);
+    } else {
+        p1 = transform_vertex(mesh, M, i1); p2 = transform_vertex(mesh, M, i2); p3 = transform_vertex(mesh, M, i3);
+    }
+}
+
 // One triangle of the draw (t >= mesh.ntri: none; every lane of the warp calls it for the
 // warp-wide steps): its record, its small-triangle tile counts or large-queue slot, and the
 // direct folds of the smallest triangles.
@@ -75,22 +95,10 @@ __device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4
     DirectWalk dw{false, 0, 0u};
     const Viewport vp = to_vp(g);
     if (live) {
-        uint32_t i1, i2, i3;
-        if (mesh.idx) {
-            i1 = __ldg(mesh.idx + 3 * (size_t)t + 0);
-            i2 = __ldg(mesh.idx + 3 * (size_t)t + 1);
-            i3 = __ldg(mesh.idx + 3 * (size_t)t + 2);
-        } else {
-            i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
-        }
-        const int dmax = kDirect ? g.direct_max : 0;
-        DirectWalk *dwp = kDirect ? &dw : nullptr;
-        if (tv)
-            r = build_record(__ldg(tv + i1), __ldg(tv + i2), __ldg(tv + i3), mesh.rgb + 3 * (size_t)t, g.w, g.h,
-                             dmax, dwp);
-        else
-            r = build_record(transform_vertex(mesh, M, i1), transform_vertex(mesh, M, i2),
-                             transform_vertex(mesh, M, i3), mesh.rgb + 3 * (size_t)t, g.w, g.h, dmax, dwp);
+        float4 p1, p2, p3;
+        triangle_vertices(mesh, tv, M, t, p1, p2, p3);
+        r = build_record(p1, p2, p3, mesh.rgb + 3 * (size_t)t, g.w, g.h, kDirect ? g.direct_max : 0,
+                         kDirect ? &dw : nullptr);
         sp = tile_span(vp, r);
         store_record(fb.records + tri_base + t, r, sp.ntiles);
         direct = dw.direct;
@@ -113,17 +121,40 @@ __device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4
     }
 }
 
-// tv null (soups): each thread transforms its triangle's three vertices itself, which
-// saves the vertex kernel and its round trip through memory.
+// A block takes tpb triangles in two phases.  Phase 1: every triangle gets its sample range
+// and the back-face proof (needs_setup); those with nothing to rasterize store their range
+// row and are done, the others are queued in shared memory.  Phase 2: the queued
+// triangles, dense in the lanes, get the rest of their setup (setup_triangle).  Back faces
+// are about half of a closed mesh's triangles, and mixed through every warp: without the
+// queue half the lanes of a warp would idle through the front faces' work.
 // kDirect: compiled with the direct path (g.direct_max > 0), which needs more registers.
 template <bool kDirect>
 __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFillMinBlocks)
 setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_base, FrameGeom g,
              FrameBuffers fb, BinBuffers bb, int tpb)
 {
-    for (uint32_t t = blockIdx.x * (uint32_t)tpb + threadIdx.x; t < (blockIdx.x + 1u) * (uint32_t)tpb;
-         t += blockDim.x)
-        setup_triangle<kDirect>(mesh, tv, M, tri_base, g, fb, bb, t);
+    __shared__ uint32_t squeue[kMaxTrianglesPerBlock];
+    __shared__ uint32_t sq_n;
+    if (threadIdx.x == 0) sq_n = 0;
+    block_sync();
+    const uint32_t t0 = blockIdx.x * (uint32_t)tpb;
+    for (uint32_t t = t0 + threadIdx.x; t < t0 + (uint32_t)tpb; t += blockDim.x) {
+        bool keep = false;
+        if (t < mesh.ntri) {
+            float4 p1, p2, p3;
+            triangle_vertices(mesh, tv, M, t, p1, p2, p3);
+            int4 row4;
+            keep = needs_setup(p1, p2, p3, g.w, g.h, row4);
+            if (!keep) reinterpret_cast<int4 *>(fb.records + tri_base + t)[4] = row4;
+        }
+        queue_push(keep, t, squeue, &sq_n);
+    }
+    block_sync();
+    const uint32_t nq = sq_n;
+    for (uint32_t base = 0; base < nq; base += blockDim.x) {
+        const uint32_t q = base + threadIdx.x;
+        setup_triangle<kDirect>(mesh, tv, M, tri_base, g, fb, bb, q < nq ? squeue[q] : 0xffffffffu);
+    }
 }
 
 // Newline sentinels (src/rasterizer.rs:89-91): in image mode every row y in [y0,y1) of

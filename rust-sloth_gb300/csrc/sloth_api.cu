@@ -231,7 +231,7 @@ static sloth_status alloc_frame(sloth_ctx *ctx)
     CU(ctx, dalloc(&ctx->bb.tile_count, ntiles));
     CU(ctx, dalloc(&ctx->bb.tile_offset, ntiles + 1));
     CU(ctx, dalloc(&ctx->bb.tile_cursor, ntiles));
-    CU(ctx, dalloc(&ctx->bb.slice_offset, ntiles + 4));
+    CU(ctx, dalloc(&ctx->bb.slice_offset, ntiles + kSliceExtra));
     ctx->ntiles_cap = (uint32_t)ntiles;
     ctx->fb.gen = 0;
     ctx->g = g;

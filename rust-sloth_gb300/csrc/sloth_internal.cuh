@@ -29,6 +29,19 @@ __device__ __forceinline__ void block_sync()
     __syncthreads();
 }
 
+// Appends v to a shared-memory queue when keep holds, one shared atomic per warp (called
+// by all 32 lanes of the warp).
+__device__ __forceinline__ void queue_push(bool keep, uint32_t v, uint32_t *queue, uint32_t *count)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) queue[base + __popc(m & ((1u << lane) - 1u))] = v;
+}
+
 constexpr float kFltMax = 3.40282347e+38f;
 constexpr uint64_t kEmptyKey = ~0ull;
 constexpr uint32_t kSmallMaxTilesDev = 16;   // triangles over more tiles are binned by warps

@@ -49,9 +49,12 @@ struct BinBuffers {
                              // ones from the front, the others from the back (bin_common.cuh)
     uint32_t *large_count;   // 2: big triangles queued, other large triangles queued
     uint32_t large_cap;
-    uint32_t *slice_offset;  // ntiles + 4: per tile the first raster item of its slices;
-                             // [ntiles] = items, [ntiles+1] = split threshold, [ntiles+2] =
-                             // slice size, [ntiles+3] = items of split tiles (listed first)
+    uint32_t *slice_offset;  // ntiles + kSliceExtra: per tile the first raster item of its
+                             // slices within its class (item_offset); [ntiles] = items,
+                             // [ntiles+1] = split threshold, [ntiles+2] = slice size,
+                             // [ntiles+3] = items of split tiles (listed first), [ntiles+4] =
+                             // first item of the light tiles (listed last), [ntiles+5] = the
+                             // light threshold (entries)
     uint2 *items;            // item_capacity: (tile, slice) of each raster CTA
     uint32_t item_capacity;
     uint32_t *max_total;     // optional: the scan folds each draw's entry total in (atomicMax)
@@ -76,6 +79,17 @@ struct SplitParams {
 __host__ __device__ inline uint32_t tile_slices(uint32_t n, SplitParams sp)
 {
     return n == 0 ? 0u : (n <= sp.threshold ? 1u : (n + sp.slice - 1) / sp.slice);
+}
+
+constexpr uint32_t kSliceExtra = 6;   // entries of slice_offset past the tiles
+
+// The first raster item of tile t (cnt entries) among the three classes the scan numbers:
+// split tiles' slices, then the other tiles, then the light ones.
+__host__ __device__ inline uint32_t item_offset(const uint32_t *so, uint32_t ntiles, uint32_t t, uint32_t cnt,
+                                               uint32_t split_threshold)
+{
+    const uint32_t base = cnt > split_threshold ? 0u : (cnt < so[ntiles + 5] ? so[ntiles + 4] : so[ntiles + 3]);
+    return so[t] + base;
 }
 
 // Raster CTAs needed for ntiles tiles holding at most `capacity` entries in total.
@@ -104,6 +118,7 @@ constexpr int kSetupMinBlocks = 3;   // resident setup blocks per SM the registe
 constexpr int kFillMinBlocks = 4;    // the same for the fill kernels and setup without the direct path
 constexpr int kDefaultTrianglesPerBlock = 256;
 constexpr int kTrianglesPerBlockChoices[4] = {128, 256, 1024, 4096};
+constexpr int kMaxTrianglesPerBlock = 4096;
 inline bool valid_triangles_per_block(long long v) { return v == 128 || v == 256 || v == 1024 || v == 4096; }
 __host__ __device__ inline int setup_block_threads(int tpb) { return tpb < kSetupThreads ? tpb : kSetupThreads; }
 
