@@ -133,16 +133,21 @@ __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFi
     const int2 blk = blocks[blockIdx.x];
     const BatchDraw &d = b.draws[blk.x];
     const BatchFrame &f = b.frames[d.frame];
-    for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < (uint32_t)blk.y + (uint32_t)b.tpb; t += blockDim.x) {
-        bool keep = false;
-        if (t < d.mesh.ntri) {
-            float4 p1, p2, p3;
-            batch_triangle_vertices(b, d, t, p1, p2, p3);
-            int4 row4;
-            keep = needs_setup(p1, p2, p3, f.g.w, f.g.h, row4);
-            if (!keep) reinterpret_cast<int4 *>(f.fb.records + d.local_base + t)[4] = row4;
-        }
-        queue_push(keep, t, squeue, &sq_n);
+    const uint32_t end = (uint32_t)blk.y + (uint32_t)b.tpb;
+    // two triangles per round, their vertex loads issued together
+    for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < end; t += 2 * blockDim.x) {
+        const uint32_t u = t + blockDim.x;
+        const bool lt = t < d.mesh.ntri, lu = u < end && u < d.mesh.ntri;
+        float4 a1, a2, a3, b1, b2, b3;
+        if (lt) batch_triangle_vertices(b, d, t, a1, a2, a3);
+        if (lu) batch_triangle_vertices(b, d, u, b1, b2, b3);
+        int4 row4;
+        const bool kt = lt && needs_setup(a1, a2, a3, f.g.w, f.g.h, row4);
+        if (lt && !kt) reinterpret_cast<int4 *>(f.fb.records + d.local_base + t)[4] = row4;
+        const bool ku = lu && needs_setup(b1, b2, b3, f.g.w, f.g.h, row4);
+        if (lu && !ku) reinterpret_cast<int4 *>(f.fb.records + d.local_base + u)[4] = row4;
+        queue_push(kt, t, squeue, &sq_n);
+        queue_push(ku, u, squeue, &sq_n);
     }
     block_sync();
     const uint32_t nq = sq_n;

@@ -138,16 +138,20 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
     if (threadIdx.x == 0) sq_n = 0;
     block_sync();
     const uint32_t t0 = blockIdx.x * (uint32_t)tpb;
-    for (uint32_t t = t0 + threadIdx.x; t < t0 + (uint32_t)tpb; t += blockDim.x) {
-        bool keep = false;
-        if (t < mesh.ntri) {
-            float4 p1, p2, p3;
-            triangle_vertices(mesh, tv, M, t, p1, p2, p3);
-            int4 row4;
-            keep = needs_setup(p1, p2, p3, g.w, g.h, row4);
-            if (!keep) reinterpret_cast<int4 *>(fb.records + tri_base + t)[4] = row4;
-        }
-        queue_push(keep, t, squeue, &sq_n);
+    // two triangles per round, their vertex loads issued together
+    for (uint32_t t = t0 + threadIdx.x; t < t0 + (uint32_t)tpb; t += 2 * blockDim.x) {
+        const uint32_t u = t + blockDim.x;
+        const bool lt = t < mesh.ntri, lu = u < t0 + (uint32_t)tpb && u < mesh.ntri;
+        float4 a1, a2, a3, b1, b2, b3;
+        if (lt) triangle_vertices(mesh, tv, M, t, a1, a2, a3);
+        if (lu) triangle_vertices(mesh, tv, M, u, b1, b2, b3);
+        int4 row4;
+        const bool kt = lt && needs_setup(a1, a2, a3, g.w, g.h, row4);
+        if (lt && !kt) reinterpret_cast<int4 *>(fb.records + tri_base + t)[4] = row4;
+        const bool ku = lu && needs_setup(b1, b2, b3, g.w, g.h, row4);
+        if (lu && !ku) reinterpret_cast<int4 *>(fb.records + tri_base + u)[4] = row4;
+        queue_push(kt, t, squeue, &sq_n);
+        queue_push(ku, u, squeue, &sq_n);
     }
     block_sync();
     const uint32_t nq = sq_n;
