@@ -320,8 +320,13 @@ static_assert(kBatchResolveChunk % (kBatchRun * 256) == 0, "whole runs, the same
 
 __global__ void __launch_bounds__(256) batch_resolve_kernel(BatchDev b, const int2 *__restrict__ blocks)
 {
+    // the frame's descriptor in shared memory: read there, its fields are not reloaded
+    // from global memory after each of the block's output stores
+    __shared__ BatchFrame sf;
     const int2 blk = blocks[blockIdx.x];
-    const BatchFrame &f = b.frames[blk.x];
+    if (threadIdx.x == 0) sf = b.frames[blk.x];
+    block_sync();
+    const BatchFrame &f = sf;
     const uint64_t nz = (uint64_t)f.g.w * f.g.h;
     const uint64_t ncells = f.g.image ? nz + f.g.h : nz;
     const uint64_t end = min(ncells, (uint64_t)blk.y + kBatchResolveChunk);   // chunks start on runs
