@@ -70,9 +70,9 @@ __device__ __forceinline__ void batch_triangle_vertices(const BatchDev &b, const
 }
 
 template <bool kDirect>
-__device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const BatchDraw &d, uint32_t t)
+__device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const BatchDraw &d, const BatchFrame &f,
+                                                     uint32_t t)
 {
-    const BatchFrame &f = b.frames[d.frame];
     bool large = false, direct = false;
     DirectWalk dw{false, 0, 0u};
     const bool live = t < d.mesh.ntri;
@@ -128,11 +128,19 @@ __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFi
 {
     __shared__ uint32_t squeue[kMaxTrianglesPerBlock];
     __shared__ uint32_t sq_n;
-    if (threadIdx.x == 0) sq_n = 0;
-    block_sync();
+    // the draw's and frame's descriptors in shared memory: read there, their fields are not
+    // reloaded from global memory after each of the block's record stores
+    __shared__ BatchDraw sd;
+    __shared__ BatchFrame sf;
     const int2 blk = blocks[blockIdx.x];
-    const BatchDraw &d = b.draws[blk.x];
-    const BatchFrame &f = b.frames[d.frame];
+    if (threadIdx.x == 0) {
+        sq_n = 0;
+        sd = b.draws[blk.x];
+        sf = b.frames[sd.frame];
+    }
+    block_sync();
+    const BatchDraw &d = sd;
+    const BatchFrame &f = sf;
     const uint32_t end = (uint32_t)blk.y + (uint32_t)b.tpb;
     // two triangles per round, their vertex loads issued together
     for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < end; t += 2 * blockDim.x) {
@@ -153,7 +161,7 @@ __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFi
     const uint32_t nq = sq_n;
     for (uint32_t base = 0; base < nq; base += blockDim.x) {
         const uint32_t q = base + threadIdx.x;
-        batch_setup_triangle<kDirect>(b, d, q < nq ? squeue[q] : 0xffffffffu);
+        batch_setup_triangle<kDirect>(b, d, f, q < nq ? squeue[q] : 0xffffffffu);
     }
 }
 
