@@ -350,8 +350,7 @@ def run_gpu(args):
     launches = ctx.launch_count() - launches0
     ms = sum(a.elapsed_time(b) for a, b in evs)
     kernels = {}
-    for name in ("reset", "vertex", "setup", "direct", "newline", "bin_count_large", "bin_scan", "bin_fill",
-                 "bin_fill_large", "bin_items", "raster", "resolve"):
+    for name in ("reset", "vertex", "setup", "newline", "bin_count_large", "bin_scan", "bin_fill", "bin_fill_large", "bin_items", "raster", "resolve"):
         t, n = ctx.kernel_time(name)
         if n:
             kernels[name] = {"ms_per_launch": t / n, "launches": n}

@@ -375,8 +375,7 @@ sloth_status sloth_render_noalloc(const float *x, const float *y, const float *z
 /* Enable (1) / disable (0) CUDA-event timing of each kernel the context launches.
  * sloth_ctx_kernel_time() then reports the summed device time (ms) and launch count
  * of kernel `name` ("setup", "bin_count_large", "bin_scan", "bin_fill", "bin_fill_large",
- * "bin_items", "raster", "resolve", "direct") since timing was enabled; blocks until the events
- * complete. */
+ * "bin_items", "raster", "resolve") since timing was enabled; blocks until the events complete. */
 sloth_status sloth_ctx_set_timing(sloth_ctx *ctx, int enable);
 sloth_status sloth_ctx_kernel_time(sloth_ctx *ctx, const char *name, double *ms, uint64_t *launches);
 /* Number of kernels launched by this context since creation. */

@@ -907,8 +907,7 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
                   ctx->nl_stream));
     CU(ctx, cudaEventRecord(ctx->nl_ev, ctx->nl_stream));
     ctx->nl_pending = true;
-    if (g.direct_max > 0)
-        CU(ctx, timed(ctx, "direct", [&] { return launch_direct(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
+    CU(ctx, timed(ctx, "direct", [&] { return launch_direct(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_count_large",[&] { return launch_bin_count_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
     // The entry count is known only on the device.  With an entry buffer from earlier draws
