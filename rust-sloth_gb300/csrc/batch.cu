@@ -107,37 +107,13 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
             b.large_frame[q] = d.frame;
         }
     }
-    // the smallest triangles are listed for batch_direct_kernel, one atomic per warp
-    if (kDirect) {
-        const unsigned dm = __ballot_sync(0xffffffffu, direct);
-        if (dm) {
-            const int lane = threadIdx.x & 31;
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(b.direct_count, (uint32_t)__popc(dm));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (direct) b.direct_list[base + __popc(dm & ((1u << lane) - 1u))] = make_uint2(d.frame, d.local_base + t);
-        }
-    }
-}
-
-// The direct triangles setup listed, one per lane (grid-stride): each folds its covered
-// samples straight into its frame's global keys (direct.cuh), walked as build_record sized it
-// (direct_walk_of).  The frames share one fragment counter.
-__global__ void __launch_bounds__(256) batch_direct_kernel(BatchDev b)
-{
-    const uint32_t n = *b.direct_count;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
-        uint32_t frags = 0;
-        if (i < n) {
-            const uint2 e = b.direct_list[i];
-            const BatchFrame &f = b.frames[e.x];
-            const TriRecord r = load_record(f.fb.records, e.y);
-            const DirectWalk dw = direct_walk_of(r, f.g.w);
-            frags = direct_raster(r, e.y, f.g.w, f.g.pitch, reinterpret_cast<unsigned long long *>(f.fb.keys), dw.xend,
-                                  dw.exit_mask);
-        }
-        add_frags_warp(frags, b.frames[0].fb.fragments);
+    // the smallest triangles fold their samples into the frame's global keys (direct.cuh)
+    if (kDirect && __any_sync(0xffffffffu, direct)) {
+        const uint32_t frags = direct ? direct_raster(r, d.local_base + t, f.g.w, f.g.pitch,
+                                                      reinterpret_cast<unsigned long long *>(f.fb.keys), dw.xend,
+                                                      dw.exit_mask)
+                                      : 0u;
+        add_frags_warp(frags, f.fb.fragments);
     }
 }
 
@@ -148,7 +124,7 @@ __global__ void __launch_bounds__(256) batch_direct_kernel(BatchDev b)
 // setup's two phases (setup.cu): the range and the back-face proof for every triangle, the
 // rest of the setup for the ones queued in shared memory.
 template <bool kDirect>
-__global__ void __launch_bounds__(kSetupThreads, kFillMinBlocks) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
+__global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFillMinBlocks) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
 {
     __shared__ uint32_t squeue[kMaxTrianglesPerBlock];
     __shared__ uint32_t sq_n;
@@ -406,13 +382,6 @@ cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s)
     const int grid = 8 * device_sm_count();   // eight CTAs of 8 warps per SM; the warps stride over the items
     if (fill) batch_bin_large_kernel<true><<<grid, 256, 0, s>>>(b);
     else batch_bin_large_kernel<false><<<grid, 256, 0, s>>>(b);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_batch_direct(const BatchDev &b, cudaStream_t s)
-{
-    if (b.direct_max <= 0 || !b.nframes) return cudaSuccess;
-    batch_direct_kernel<<<8 * device_sm_count(), 256, 0, s>>>(b);
     return cudaGetLastError();
 }
 

@@ -66,8 +66,6 @@ struct sloth_batch {
     uint32_t *queue = nullptr;                // the persistent raster's item counter
     uint2 *fill_list = nullptr;               // the fill's work list (one entry per record at most)
     uint32_t *fill_count = nullptr;
-    uint2 *direct_list = nullptr;             // the direct kernel's work list
-    uint32_t *direct_count = nullptr;
     uint32_t *h_total = nullptr;              // pinned
     uint32_t *h_overflow = nullptr;           // pinned
     uint32_t *error = nullptr;                // device error word of the raster (sticky)
@@ -165,8 +163,6 @@ void free_layout(sloth_batch *b)
     bfree(b->queue);
     bfree(b->fill_list);
     bfree(b->fill_count);
-    bfree(b->direct_list);
-    bfree(b->direct_count);
     for (auto &p : b->blk) bfree(p);
     b->entries_cap = 0;
     b->rendered = false;
@@ -290,8 +286,6 @@ sloth_status build(sloth_batch *b, int shape)
     BCU(b, balloc(&b->queue, 1));
     BCU(b, balloc(&b->fill_list, rec));
     BCU(b, balloc(&b->fill_count, 1));
-    BCU(b, balloc(&b->direct_list, rec));
-    BCU(b, balloc(&b->direct_count, 1));
     BCU(b, balloc(&b->d_mats, nd));
     for (uint32_t f = 0; f < nf; ++f) {
         BatchFrame &bf = b->hframes[f];
@@ -340,8 +334,6 @@ BatchDev dev_view(sloth_batch *b)
     d.queue = b->queue;
     d.fill_list = b->fill_list;
     d.fill_count = b->fill_count;
-    d.direct_list = b->direct_list;
-    d.direct_count = b->direct_count;
     d.depth_cull = sloth_ctx_depth_cull(b->ctx);
     d.tpb = b->tpb;
     d.direct_max = b->direct_max;
@@ -364,7 +356,6 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     if ((e = cudaMemsetAsync(b->nltree, 0xff, (size_t)b->total_nl * 4, s))) return e;
     if ((e = cudaMemsetAsync(b->bb.large_count, 0, 8, s))) return e;
     if ((e = cudaMemsetAsync(b->fill_count, 0, 4, s))) return e;
-    if ((e = cudaMemsetAsync(b->direct_count, 0, 4, s))) return e;
     if ((e = cudaMemsetAsync(b->fragments, 0, 8, s))) return e;
     if ((e = cudaMemsetAsync(b->overflow, 0, 4, s))) return e;
     if ((e = cudaMemcpyAsync(b->d_mats, b->h_mats, b->meshes.size() * sizeof(Mat4), cudaMemcpyHostToDevice, s)))
@@ -375,7 +366,6 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     if ((e = cudaStreamWaitEvent(b->nl_s, b->ev_setup, 0))) return e;
     if ((e = launch_batch_newline(d, b->blk[2], b->nblk[2], b->max_nl, b->nl_s))) return e;
     if ((e = cudaEventRecord(b->ev_nl, b->nl_s))) return e;
-    if ((e = launch_batch_direct(d, s))) return e;
     if ((e = launch_batch_bin_large(d, false, s))) return e;
     return launch_bin_scan(b->total_tiles, d.bb, s);
 }

@@ -49,9 +49,6 @@ struct BatchDev {
     uint2 *fill_list;          // (frame, frame-local draw index) of every small binned triangle,
                                // appended by setup: the fill walks only these
     uint32_t *fill_count;      // entries of fill_list (zeroed at the start of a render)
-    uint2 *direct_list;        // (frame, frame-local draw index) of every direct triangle,
-                               // appended by setup: batch_direct_kernel folds their samples
-    uint32_t *direct_count;    // entries of direct_list (zeroed at the start of a render)
     int depth_cull;
     int tpb;                   // triangles per setup/fill block (the triangle block table's step)
     int direct_max;            // the frames' FrameGeom::direct_max (the same for every frame)
@@ -64,7 +61,6 @@ cudaError_t launch_batch_newline(const BatchDev &b, const int2 *blocks, uint32_t
                                  cudaStream_t s);
 cudaError_t launch_batch_bin_large(const BatchDev &b, bool fill, cudaStream_t s);
 cudaError_t launch_batch_fill(const BatchDev &b, cudaStream_t s);
-cudaError_t launch_batch_direct(const BatchDev &b, cudaStream_t s);
 cudaError_t launch_batch_items(const BatchDev &b, cudaStream_t s);
 cudaError_t launch_batch_raster(const BatchDev &b, int tw, int th, bool persistent, cudaStream_t s);
 cudaError_t launch_batch_resolve(const BatchDev &b, const int2 *blocks, uint32_t nblocks, cudaStream_t s);

@@ -70,29 +70,6 @@ __device__ __forceinline__ int sat_hi(float f)
     return f > 0.0f ? (int)f : 0;
 }
 
-// How the setup thread rasterizes a direct triangle (direct.cuh): its samples lie in rows
-// [y0,y1) from column x0, up to column xend (exclusive); with exit_mask set, a row ends at
-// the first column where an edge in the mask (bit i: edge i, those with dy > 0) is negative.
-struct DirectWalk {
-    bool direct;
-    int xend;
-    uint32_t exit_mask;
-};
-
-// The walk of a direct triangle rebuilt from its stored record, with build_record's
-// operations: a finite triangle with an edge of dy > 0 was sized by its unproven right end
-// and is walked up to the reference's bound with early row exits; any other direct
-// triangle is walked over its stored range.
-__device__ __forceinline__ DirectWalk direct_walk_of(const TriRecord &r, int w)
-{
-    const uint32_t mask = (r.dy0 > 0.0f ? 1u : 0u) | (r.dy1 > 0.0f ? 2u : 0u) | (r.dy2 > 0.0f ? 4u : 0u);
-    if ((r.flags & kFlagFiniteXY) && mask) {
-        const float mxx = fmaxf(r.v1x, fmaxf(r.v2x, r.v3x));
-        return DirectWalk{true, sat_hi(ceilf(fminf(fmul(mxx, 2.0f), (float)(w - 1)))), mask};
-    }
-    return DirectWalk{true, r.xe, 0u};
-}
-
 // Stores a record.  A triangle with no tile (culled, empty sample range) only ever has its
 // sample range read -- by the newline and fill kernels, which stop there -- so only that
 // row is written.
@@ -135,7 +112,14 @@ __device__ __forceinline__ bool needs_setup(float4 p1, float4 p2, float4 p3, int
     return true;
 }
 
-
+// How the setup thread rasterizes a direct triangle (direct.cuh): its samples lie in rows
+// [y0,y1) from column x0, up to column xend (exclusive); with exit_mask set, a row ends at
+// the first column where an edge in the mask (bit i: edge i, those with dy > 0) is negative.
+struct DirectWalk {
+    bool direct;
+    int xend;
+    uint32_t exit_mask;
+};
 
 // The record of one triangle with transformed vertices p1, p2, p3 (xyz) and face colour
 // c[0..2] in a w x h context.  With direct_max > 0, a triangle whose sample range holds at

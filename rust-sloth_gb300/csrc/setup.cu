@@ -9,7 +9,6 @@
 
 #include "bin_common.cuh"
 #include "direct.cuh"
-#include "raster_common.cuh"
 #include "record.cuh"
 #include "sloth_kernels.h"
 
@@ -112,44 +111,14 @@ __device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4
         const int q = large_slot(large, sp.ntiles, bb.large_count, bb.large_cap);
         if (q >= 0) bb.large_queue[q] = t;
     }
-    // the smallest triangles are listed for direct_kernel, one atomic per warp
-    if (kDirect) {
-        const unsigned dm = __ballot_sync(0xffffffffu, direct);
-        if (dm) {
-            const int lane = threadIdx.x & 31;
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(bb.direct_count, (uint32_t)__popc(dm));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (direct) bb.direct_list[base + __popc(dm & ((1u << lane) - 1u))] = t;
-        }
-    }
-}
-
-// The direct triangles setup listed, one per lane (grid-stride): each folds its covered
-// samples straight into the global keys (direct.cuh), walked as build_record sized it.
-__global__ void __launch_bounds__(256) direct_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
-{
-    const uint32_t n = *bb.direct_count;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
-        uint32_t frags = 0;
-        if (i < n) {
-            const uint32_t gtri = tri_base + bb.direct_list[i];
-            const TriRecord r = load_record(fb.records, gtri);
-            const DirectWalk dw = direct_walk_of(r, g.w);
-            frags = direct_raster(r, gtri, g.w, g.pitch, reinterpret_cast<unsigned long long *>(fb.keys), dw.xend,
-                                  dw.exit_mask);
-        }
+    // the smallest triangles fold their samples into the global keys here (direct.cuh)
+    if (kDirect && __any_sync(0xffffffffu, direct)) {
+        const uint32_t frags = direct ? direct_raster(r, tri_base + t, g.w, g.pitch,
+                                                      reinterpret_cast<unsigned long long *>(fb.keys), dw.xend,
+                                                      dw.exit_mask)
+                                      : 0u;
         add_frags_warp(frags, fb.fragments);
     }
-}
-
-cudaError_t launch_direct(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
-                          cudaStream_t s)
-{
-    if (g.direct_max <= 0) return cudaSuccess;
-    direct_kernel<<<4 * device_sm_count(), 256, 0, s>>>(tri_base, g, fb, bb);
-    return cudaGetLastError();
 }
 
 // A block takes tpb triangles in two phases.  Phase 1: every triangle gets its sample range
@@ -158,9 +127,9 @@ cudaError_t launch_direct(uint32_t tri_base, const FrameGeom &g, const FrameBuff
 // triangles, dense in the lanes, get the rest of their setup (setup_triangle).  Back faces
 // are about half of a closed mesh's triangles, and mixed through every warp: without the
 // queue half the lanes of a warp would idle through the front faces' work.
-// kDirect: compiled with the direct path (g.direct_max > 0): its triangles are listed.
+// kDirect: compiled with the direct path (g.direct_max > 0), which needs more registers.
 template <bool kDirect>
-__global__ void __launch_bounds__(kSetupThreads, kFillMinBlocks)
+__global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFillMinBlocks)
 setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_base, FrameGeom g,
              FrameBuffers fb, BinBuffers bb, int tpb)
 {
@@ -252,7 +221,6 @@ frame_reset_kernel(FrameBuffers fb, BinBuffers bb, uint32_t nl_nodes, uint32_t n
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (frame && i < nl_nodes) fb.nltree[i] = -1;
     if (draw && i < ntiles) bb.tile_count[i] = 0u;
-    if (draw && i == 0 && bb.direct_count) *bb.direct_count = 0u;
     if (tiles_current && i < ntiles) fb.tile_gen[i] = fb.gen;
     if (i == 0) {
         if (frame) {

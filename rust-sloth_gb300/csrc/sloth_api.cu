@@ -70,7 +70,6 @@ struct sloth_ctx {
     BinBuffers bb{};
     uint32_t ntiles_cap = 0;
     size_t large_cap = 0;
-    size_t direct_cap = 0;
     float4 *tv = nullptr;
     size_t tv_cap = 0;
     uint32_t *h_total = nullptr;   // pinned
@@ -525,8 +524,6 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     dfree(ctx->bb.entries);
     dfree(ctx->bb.large_queue);
     dfree(ctx->bb.large_count);
-    dfree(ctx->bb.direct_list);
-    dfree(ctx->bb.direct_count);
     dfree(ctx->bb.items);
     dfree(ctx->tv);
     if (ctx->h_total) cudaFreeHost(ctx->h_total);
@@ -880,10 +877,6 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     if ((st = ensure_records(ctx, (size_t)ctx->tri_base + mesh->ntri)) != SLOTH_OK) return st;
     if (mesh->idx && (st = ensure_scratch(ctx, &ctx->tv, &ctx->tv_cap, mesh->nvert)) != SLOTH_OK) return st;
     if ((st = ensure_scratch(ctx, &ctx->bb.large_queue, &ctx->large_cap, mesh->ntri)) != SLOTH_OK) return st;
-    if (ctx->g.direct_max > 0 &&
-        (st = ensure_scratch(ctx, &ctx->bb.direct_list, &ctx->direct_cap, mesh->ntri)) != SLOTH_OK)
-        return st;
-    if (!ctx->bb.direct_count) CU(ctx, dalloc(&ctx->bb.direct_count, 1));
     if (!ctx->bb.large_count) CU(ctx, dalloc(&ctx->bb.large_count, 2));
     ctx->bb.large_cap = mesh->ntri;
 
@@ -907,7 +900,6 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
                   ctx->nl_stream));
     CU(ctx, cudaEventRecord(ctx->nl_ev, ctx->nl_stream));
     ctx->nl_pending = true;
-    CU(ctx, timed(ctx, "direct", [&] { return launch_direct(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_count_large",[&] { return launch_bin_count_large(ctx->tri_base, g, ctx->fb, ctx->bb, s); }));
     CU(ctx, timed(ctx, "bin_scan", [&] { return launch_bin_scan(ntiles, ctx->bb, s); }));
     // The entry count is known only on the device.  With an entry buffer from earlier draws

@@ -58,8 +58,6 @@ struct BinBuffers {
     uint2 *items;            // item_capacity: (tile, slice) of each raster CTA
     uint32_t item_capacity;
     uint32_t *max_total;     // optional: the scan folds each draw's entry total in (atomicMax)
-    uint32_t *direct_list;   // draw-local indices of the draw's direct triangles (direct path on)
-    uint32_t *direct_count;  // entries of direct_list (zeroed by the draw's reset)
 };
 
 // A tile holding many more entries than the launch's mean is rasterized in slices by
@@ -144,10 +142,6 @@ cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *
 cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, uint32_t tri_base,
                          const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
                          cudaStream_t s, int tpb = kDefaultTrianglesPerBlock);
-// direct path: the triangles setup listed fold their covered samples straight into the
-// global keys (no launch when g.direct_max is 0).
-cudaError_t launch_direct(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
-                          cudaStream_t s);
 // newline sentinels (image mode): fold each triangle's row range into the segment tree.
 cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
                            const FrameBuffers &fb, cudaStream_t s);
