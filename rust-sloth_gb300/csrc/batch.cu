@@ -49,8 +49,6 @@ __global__ void __launch_bounds__(256) batch_vertex_kernel(BatchDev b, const int
                                      row_dot(&M.m[8], xs[k], ys[k], zs[k]), 0.0f);
 }
 
-// One triangle of draw d (every lane of the warp calls it: t >= ntri is none): record,
-// small-triangle tile counts, large queue, and the direct folds of the smallest triangles.
 // The three transformed vertices of triangle t of draw d (the vertex kernel's output).
 __device__ __forceinline__ void batch_triangle_vertices(const BatchDev &b, const BatchDraw &d, uint32_t t, float4 &p1,
                                                         float4 &p2, float4 &p3)
@@ -69,25 +67,25 @@ __device__ __forceinline__ void batch_triangle_vertices(const BatchDev &b, const
     p3 = __ldg(tv + i3);
 }
 
+// One triangle t of draw d with transformed vertices p1, p2, p3 and packed colour rgb
+// (live false: none; every lane of the warp calls it): record, small-triangle tile
+// counts, fill list or large queue, and the direct folds of the smallest triangles.
 template <bool kDirect>
 __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const BatchDraw &d, const BatchFrame &f,
-                                                     uint32_t t)
+                                                     bool live, uint32_t t, float4 p1, float4 p2, float4 p3,
+                                                     uint32_t rgb)
 {
     bool large = false, direct = false;
     DirectWalk dw{false, 0, 0u};
-    const bool live = t < d.mesh.ntri;
     TriRecord r;
     TileSpan sp{};
     const Viewport vp = vp_batch(f.g);
     if (live) {
-        float4 p1, p2, p3;
-        batch_triangle_vertices(b, d, t, p1, p2, p3);
-        r = build_record(p1, p2, p3, d.mesh.rgb + 3 * (size_t)t, f.g.w, f.g.h, kDirect ? f.g.direct_max : 0,
-                         kDirect ? &dw : nullptr);
-        sp = tile_span(vp, r);
-        store_record(f.fb.records + d.local_base + t, r, sp.ntiles);
+        r = build_record(p1, p2, p3, rgb, f.g.w, f.g.h, kDirect ? f.g.direct_max : 0, kDirect ? &dw : nullptr);
         direct = dw.direct;
-        large = sp.large && !direct;
+        if (!direct) sp = tile_span(vp, r);   // a direct triangle is not binned
+        store_record(f.fb.records + d.local_base + t, r, sp.ntiles, direct);
+        large = sp.large;
     }
     const bool binned = live && !large && !direct && sp.ntiles != 0;
     count_small_tiles_warp(binned, r, vp, sp, b.bb.tile_count + f.tile_off);
@@ -117,22 +115,20 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
     }
 }
 
-// blocks[i] = (draw, first triangle): b.tpb triangles of the draw, each thread taking
-// b.tpb / blockDim.x of them in turn.
-
 // blocks[i] = (draw, first triangle): b.tpb triangles of the draw in the single-frame
-// setup's two phases (setup.cu): the range and the back-face proof for every triangle, the
-// rest of the setup for the ones queued in shared memory.
-template <bool kDirect>
+// setup's chunks and two phases (setup.cu): the range and the back-face proof for every
+// triangle, the rest of the setup for the ones queued in shared memory with their vertices.
+template <bool kDirect, bool kChunks>
 __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFillMinBlocks) batch_setup_kernel(BatchDev b, const int2 *__restrict__ blocks)
 {
-    __shared__ uint32_t squeue[kMaxTrianglesPerBlock];
     __shared__ uint32_t sq_n;
     // the draw's and frame's descriptors in shared memory: read there, their fields are not
     // reloaded from global memory after each of the block's record stores
     __shared__ BatchDraw sd;
     __shared__ BatchFrame sf;
     const int2 blk = blocks[blockIdx.x];
+    const uint32_t cap = (uint32_t)setup_chunk(b.tpb);
+    const SetupStash st{cap};
     if (threadIdx.x == 0) {
         sq_n = 0;
         sd = b.draws[blk.x];
@@ -141,27 +137,44 @@ __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFi
     block_sync();
     const BatchDraw &d = sd;
     const BatchFrame &f = sf;
-    const uint32_t end = (uint32_t)blk.y + (uint32_t)b.tpb;
-    // two triangles per round, their vertex loads issued together
-    for (uint32_t t = (uint32_t)blk.y + threadIdx.x; t < end; t += 2 * blockDim.x) {
-        const uint32_t u = t + blockDim.x;
-        const bool lt = t < d.mesh.ntri, lu = u < end && u < d.mesh.ntri;
-        float4 a1, a2, a3, b1, b2, b3;
-        if (lt) batch_triangle_vertices(b, d, t, a1, a2, a3);
-        if (lu) batch_triangle_vertices(b, d, u, b1, b2, b3);
-        int4 row4;
-        const bool kt = lt && needs_setup(a1, a2, a3, f.g.w, f.g.h, row4);
-        if (lt && !kt) reinterpret_cast<int4 *>(f.fb.records + d.local_base + t)[4] = row4;
-        const bool ku = lu && needs_setup(b1, b2, b3, f.g.w, f.g.h, row4);
-        if (lu && !ku) reinterpret_cast<int4 *>(f.fb.records + d.local_base + u)[4] = row4;
-        queue_push(kt, t, squeue, &sq_n);
-        queue_push(ku, u, squeue, &sq_n);
-    }
-    block_sync();
-    const uint32_t nq = sq_n;
-    for (uint32_t base = 0; base < nq; base += blockDim.x) {
-        const uint32_t q = base + threadIdx.x;
-        batch_setup_triangle<kDirect>(b, d, f, q < nq ? squeue[q] : 0xffffffffu);
+    const uint32_t t0 = (uint32_t)blk.y, t_end = min(d.mesh.ntri, t0 + (uint32_t)b.tpb);
+    uint32_t base = 0;
+    for (uint32_t c0 = t0; c0 < t_end; c0 += cap) {
+        // two triangles per round, their vertex loads issued together (the same trip count
+        // in every lane)
+        for (uint32_t t = c0 + threadIdx.x; t < c0 + cap; t += 2 * blockDim.x) {
+            const uint32_t u = t + blockDim.x;
+            const bool lt = t < t_end, lu = u < c0 + cap && u < t_end;
+            float4 a1, a2, a3, b1, b2, b3;
+            uint32_t ca = 0, cb = 0;
+            if (lt) {
+                batch_triangle_vertices(b, d, t, a1, a2, a3);
+                ca = load_rgb(d.mesh.rgb, t);
+            }
+            if (lu) {
+                batch_triangle_vertices(b, d, u, b1, b2, b3);
+                cb = load_rgb(d.mesh.rgb, u);
+            }
+            int4 row4;
+            const bool kt = lt && needs_setup(a1, a2, a3, f.g.w, f.g.h, row4);
+            if (lt && !kt) reinterpret_cast<int4 *>(f.fb.records + d.local_base + t)[4] = row4;
+            stash_push(st, &sq_n, base, kt, t, a1, a2, a3, ca);
+            const bool ku = lu && needs_setup(b1, b2, b3, f.g.w, f.g.h, row4);
+            if (lu && !ku) reinterpret_cast<int4 *>(f.fb.records + d.local_base + u)[4] = row4;
+            stash_push(st, &sq_n, base, ku, u, b1, b2, b3, cb);
+        }
+        block_sync();
+        const uint32_t total = sq_n, nq = total - base;
+        for (uint32_t q0 = 0; q0 < nq; q0 += blockDim.x) {
+            const uint32_t q = q0 + threadIdx.x;
+            float4 p1, p2, p3;
+            uint32_t rgb = 0, t = 0;
+            if (q < nq) t = st.get(q, p1, p2, p3, rgb);
+            batch_setup_triangle<kDirect>(b, d, f, q < nq, t, p1, p2, p3, rgb);
+        }
+        if (!kChunks) break;
+        base = total;
+        if (c0 + cap < t_end) block_sync();   // the next chunk refills the stash
     }
 }
 
@@ -362,8 +375,16 @@ cudaError_t launch_batch_setup(const BatchDev &b, const int2 *blocks, uint32_t n
 {
     if (!nblocks) return cudaSuccess;
     if (!valid_triangles_per_block(b.tpb)) return cudaErrorInvalidValue;
-    if (b.direct_max > 0) batch_setup_kernel<true><<<nblocks, setup_block_threads(b.tpb), 0, s>>>(b, blocks);
-    else batch_setup_kernel<false><<<nblocks, setup_block_threads(b.tpb), 0, s>>>(b, blocks);
+    const size_t smem = setup_smem_bytes(b.tpb);   // at most 45,056 bytes: no opt-in needed
+    const dim3 grid(nblocks), block(setup_block_threads(b.tpb));
+    const bool chunks = b.tpb > kSetupChunk;
+    if (b.direct_max > 0) {
+        if (chunks) batch_setup_kernel<true, true><<<grid, block, smem, s>>>(b, blocks);
+        else batch_setup_kernel<true, false><<<grid, block, smem, s>>>(b, blocks);
+    } else {
+        if (chunks) batch_setup_kernel<false, true><<<grid, block, smem, s>>>(b, blocks);
+        else batch_setup_kernel<false, false><<<grid, block, smem, s>>>(b, blocks);
+    }
     return cudaGetLastError();
 }
 

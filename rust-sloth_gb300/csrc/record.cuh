@@ -72,11 +72,22 @@ __device__ __forceinline__ int sat_hi(float f)
 
 // Stores a record.  A triangle with no tile (culled, empty sample range) only ever has its
 // sample range read -- by the newline and fill kernels, which stop there -- so only that
-// row is written.
-__device__ __forceinline__ void store_record(TriRecord *dst, const TriRecord &r, uint32_t ntiles)
+// row is written.  A direct triangle (direct.cuh) is never binned nor rasterized again:
+// only the rows the resolve (0-1, 5) and the newline and fill kernels (4) read are written.
+__device__ __forceinline__ void store_record(TriRecord *dst, const TriRecord &r, uint32_t ntiles, bool direct = false)
 {
-    if (ntiles != 0) *dst = r;
-    else reinterpret_cast<int4 *>(dst)[4] = make_int4(r.x0, r.xe, r.y0, r.y1);
+    const int4 *src = reinterpret_cast<const int4 *>(&r);
+    int4 *d = reinterpret_cast<int4 *>(dst);
+    if (direct) {
+        d[0] = src[0];
+        d[1] = src[1];
+        d[4] = src[4];
+        d[5] = src[5];
+    } else if (ntiles != 0) {
+        *dst = r;
+    } else {
+        d[4] = make_int4(r.x0, r.xe, r.y0, r.y1);
+    }
 }
 
 // The first steps of build_record, for a setup kernel that sets triangles aside before the
@@ -112,6 +123,59 @@ __device__ __forceinline__ bool needs_setup(float4 p1, float4 p2, float4 p3, int
     return true;
 }
 
+// Face colour of triangle t: three bytes, packed as the record stores them.
+__device__ __forceinline__ uint32_t load_rgb(const uint8_t *rgb, uint32_t t)
+{
+    const uint8_t *c = rgb + 3 * (size_t)t;
+    return (uint32_t)__ldg(c) | ((uint32_t)__ldg(c + 1) << 8) | ((uint32_t)__ldg(c + 2) << 16);
+}
+
+// The queue between a setup block's two phases, in dynamic shared memory
+// (setup_smem_bytes): per slot the triangle index, its packed colour and its three
+// transformed vertices, as 11 arrays of cap words so that consecutive slots fall in
+// different banks.  Phase 2 reads a queued triangle from here, not from global memory.
+// Indexing the shared array itself keeps the accesses 32-bit shared ones.
+extern __shared__ uint32_t setup_smem[];
+
+struct SetupStash {
+    uint32_t cap;
+
+    __device__ __forceinline__ void put(uint32_t s, uint32_t t, float4 p1, float4 p2, float4 p3, uint32_t c) const
+    {
+        setup_smem[s] = t;
+        setup_smem[cap + s] = c;
+        const float v[9] = {p1.x, p1.y, p1.z, p2.x, p2.y, p2.z, p3.x, p3.y, p3.z};
+#pragma unroll
+        for (int k = 0; k < 9; ++k) setup_smem[(2 + k) * cap + s] = __float_as_uint(v[k]);
+    }
+    __device__ __forceinline__ uint32_t get(uint32_t s, float4 &p1, float4 &p2, float4 &p3, uint32_t &c) const
+    {
+        float v[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) v[k] = __uint_as_float(setup_smem[(2 + k) * cap + s]);
+        p1 = make_float4(v[0], v[1], v[2], 0.0f);
+        p2 = make_float4(v[3], v[4], v[5], 0.0f);
+        p3 = make_float4(v[6], v[7], v[8], 0.0f);
+        c = setup_smem[cap + s];
+        return setup_smem[s];
+    }
+};
+
+// Queues triangle t when keep holds, with one shared atomic per warp (called by all 32
+// lanes).  count is the block's running total of queued triangles and base its value when
+// the chunk began, so the chunk's slots are 0, 1, ... in the stash.
+__device__ __forceinline__ void stash_push(const SetupStash &st, uint32_t *count, uint32_t base, bool keep, uint32_t t,
+                                           float4 p1, float4 p2, float4 p3, uint32_t c)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    uint32_t first = 0;
+    if (lane == 0) first = atomicAdd(count, (uint32_t)__popc(m));
+    first = __shfl_sync(0xffffffffu, first, 0) - base;
+    if (keep) st.put(first + __popc(m & ((1u << lane) - 1u)), t, p1, p2, p3, c);
+}
+
 // How the setup thread rasterizes a direct triangle (direct.cuh): its samples lie in rows
 // [y0,y1) from column x0, up to column xend (exclusive); with exit_mask set, a row ends at
 // the first column where an edge in the mask (bit i: edge i, those with dy > 0) is negative.
@@ -121,16 +185,18 @@ struct DirectWalk {
     uint32_t exit_mask;
 };
 
-// The record of one triangle with transformed vertices p1, p2, p3 (xyz) and face colour
-// c[0..2] in a w x h context.  With direct_max > 0, a triangle whose sample range holds at
-// most direct_max samples is marked for the direct path (dw): such a triangle needs no
-// proven tight bound nor depth bounds.  A finite triangle with an edge of dy > 0 is sized
-// by its unproven right end floor(max.x)+1 (xe) and walked with early row exits up to the
-// reference's bound; any other triangle is sized and walked by its stored range.  A
-// triangle is direct exactly when is_direct(x0, xe, y0, y1, direct_max) holds for the
-// stored range, so later kernels recognise it from row 4 alone.
-__device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p3, const uint8_t *c,
-                                                  int w, int h, int direct_max = 0, DirectWalk *dw = nullptr)
+// The record of one triangle with transformed vertices p1, p2, p3 (xyz) and packed face
+// colour rgb (load_rgb) in a w x h context, for a triangle needs_setup kept: a triangle
+// with an empty range or proven to cover no sample over it (back faces) never gets here,
+// so the back-face proof is not repeated.  With direct_max > 0, a triangle whose sample
+// range holds at most direct_max samples is marked for the direct path (dw): such a
+// triangle needs no proven tight bound nor depth bounds.  A finite triangle with an edge
+// of dy > 0 is sized by its unproven right end floor(max.x)+1 (xe) and walked with early
+// row exits up to the reference's bound; any other triangle is sized and walked by its
+// stored range.  A triangle is direct exactly when is_direct(x0, xe, y0, y1, direct_max)
+// holds for the stored range, so later kernels recognise it from row 4 alone.
+__device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p3, uint32_t rgb, int w, int h,
+                                                  int direct_max = 0, DirectWalk *dw = nullptr)
 {
     TriRecord r;
     r.v1x = p1.x; r.v1y = p1.y; r.v2x = p2.x; r.v2y = p2.y; r.v3x = p3.x; r.v3y = p3.y;
@@ -150,7 +216,7 @@ __device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p
     const float norm2 = fadd(fadd(fmul(nx, nx), fmul(nz, nz)), fadd(fmul(ny, ny), fmul(0.0f, 0.0f)));
     const float n = __fsqrt_rn(fadd(0.0f, norm2));
     r.na = fmul(__fdiv_rn(nz, n), r.a);
-    r.rgb = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16);
+    r.rgb = rgb;
     // aabb and sample range  (src/geometry.rs:37-42, src/rasterizer.rs:59-66)
     const float mnx = fminf(p1.x, fminf(p2.x, p3.x)), mny = fminf(p1.y, fminf(p2.y, p3.y));
     const float mxx = fmaxf(p1.x, fmaxf(p2.x, p3.x)), mxy = fmaxf(p1.y, fmaxf(p2.y, p3.y));
@@ -166,13 +232,6 @@ __device__ __forceinline__ TriRecord build_record(float4 p1, float4 p2, float4 p
     r.zlo = -INFINITY;
     if (dw) *dw = DirectWalk{false, 0, 0u};
     if (finite && r.x0 < x1 && r.y0 < r.y1) {
-        // back faces first: the bounds over the untightened range hold over any subrange,
-        // so a triangle proven empty here needs no tighter range
-        if (provably_empty(orient_bound(r))) {
-            r.xe = r.x0;
-            r.flags |= kFlagCulled;
-            return r;
-        }
         if (direct_max > 0) {
             // Along a row an edge of dy > 0 is non-increasing in x (monotone correctly
             // rounded steps, finite values): once negative it stays negative, so a row walk

@@ -7,8 +7,9 @@
 //   - in image mode, the newline sentinel of row y when c == y*w+1
 // The last accepted depth write of a cell is its minimum key.  Draw order is compared
 // as (triangle, sample row, sample column); a newline comes after every sample of its
-// row.  The winner's depth, shade and char are recomputed from its record with the
-// raster's exact operations, which also restores the sign of a -0.0 depth.
+// row.  The winner's depth is its key's (the record's depth plane gives the sign of a zero
+// depth), its shade and char are recomputed from its record with the raster's exact
+// operations.
 #pragma once
 
 #include <climits>
@@ -55,17 +56,29 @@ __device__ __forceinline__ Cand decode(const FrameGeom &g, const FrameBuffers &f
         c.y = r - 1;
         c.x = (cc + g.w) >> 1;
     }
-    // rows 0-3 (vertices, edges, depth) and 5 (shade, colour); row 4 is not needed
+    // rows 0-1 (one 32-byte sector): vertices, shade factor, colour; the edge deltas are
+    // the subtractions setup made (build_record)
     const float4 *p = reinterpret_cast<const float4 *>(fb.records + c.tri);
+    const float4 q0 = __ldg(p), q1 = __ldg(p + 1);
     TriRecord rec;
-    float4 *o = reinterpret_cast<float4 *>(&rec);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) o[k] = __ldg(p + k);
-    o[5] = __ldg(p + 5);
+    rec.v1x = q0.x; rec.v1y = q0.y; rec.v2x = q0.z; rec.v2y = q0.w; rec.v3x = q1.x; rec.v3y = q1.y;
+    rec.dx0 = fsub(rec.v3x, rec.v2x); rec.dy0 = fsub(rec.v3y, rec.v2y);
+    rec.dx1 = fsub(rec.v1x, rec.v3x); rec.dy1 = fsub(rec.v1y, rec.v3y);
+    rec.dx2 = fsub(rec.v2x, rec.v1x); rec.dy2 = fsub(rec.v2y, rec.v1y);
     const EdgeVals e = eval_edges(rec, (float)c.x, (float)c.y);
-    const float shade = fmul(rec.na, fadd(fadd(e.w0, e.w1), e.w2));
-    if (z_out) *z_out = interp_z(rec.v1z, rec.dz2, rec.dz3, rec.a, e.w1, e.w2);
-    c.cell = shade_char(shade) | (rec.rgb << 8);
+    const float shade = fmul(q1.z, fadd(fadd(e.w0, e.w1), e.w2));
+    if (z_out) {
+        // the key holds the depth itself, except the sign of a zero (ordered_z folds -0 into
+        // +0): only then the depth plane (row 5) is read and the depth recomputed
+        const uint32_t hi = (uint32_t)(key >> 32);
+        if (hi != ordered_z(0.0f)) {
+            *z_out = float_of_ordered(hi);
+        } else {
+            const float4 q5 = __ldg(p + 5);
+            *z_out = interp_z(q5.x, q5.y, q5.z, q5.w, e.w1, e.w2);
+        }
+    }
+    c.cell = shade_char(shade) | (__float_as_uint(q1.w) << 8);
     return c;
 }
 

@@ -80,29 +80,26 @@ __device__ __forceinline__ void triangle_vertices(const MeshDev &mesh, const flo
     }
 }
 
-// One triangle of the draw (t >= mesh.ntri: none; every lane of the warp calls it for the
-// warp-wide steps): its record, its small-triangle tile counts or large-queue slot, and the
-// direct folds of the smallest triangles.
+// One triangle of the draw with transformed vertices p1, p2, p3 and packed colour rgb
+// (live false: none; every lane of the warp calls it for the warp-wide steps): its record,
+// its small-triangle tile counts or large-queue slot, and the direct folds of the smallest
+// triangles.
 template <bool kDirect>
-__device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4 *__restrict__ tv, const Mat4 &M,
-                                               uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
-                                               const BinBuffers &bb, uint32_t t)
+__device__ __forceinline__ void setup_triangle(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
+                                               const BinBuffers &bb, bool live, uint32_t t, float4 p1, float4 p2,
+                                               float4 p3, uint32_t rgb)
 {
-    const bool live = t < mesh.ntri;
     bool large = false, direct = false;
     TriRecord r;
     TileSpan sp{};
     DirectWalk dw{false, 0, 0u};
     const Viewport vp = to_vp(g);
     if (live) {
-        float4 p1, p2, p3;
-        triangle_vertices(mesh, tv, M, t, p1, p2, p3);
-        r = build_record(p1, p2, p3, mesh.rgb + 3 * (size_t)t, g.w, g.h, kDirect ? g.direct_max : 0,
-                         kDirect ? &dw : nullptr);
-        sp = tile_span(vp, r);
-        store_record(fb.records + tri_base + t, r, sp.ntiles);
+        r = build_record(p1, p2, p3, rgb, g.w, g.h, kDirect ? g.direct_max : 0, kDirect ? &dw : nullptr);
         direct = dw.direct;
-        large = sp.large && !direct;
+        if (!direct) sp = tile_span(vp, r);   // a direct triangle is not binned
+        store_record(fb.records + tri_base + t, r, sp.ntiles, direct);
+        large = sp.large;
     }
     // binning: count tiles of small triangles here, queue the rest for warps
     count_small_tiles_warp(live && !large && !direct, r, vp, sp, bb.tile_count);
@@ -121,43 +118,64 @@ __device__ __forceinline__ void setup_triangle(const MeshDev &mesh, const float4
     }
 }
 
-// A block takes tpb triangles in two phases.  Phase 1: every triangle gets its sample range
-// and the back-face proof (needs_setup); those with nothing to rasterize store their range
-// row and are done, the others are queued in shared memory.  Phase 2: the queued
-// triangles, dense in the lanes, get the rest of their setup (setup_triangle).  Back faces
-// are about half of a closed mesh's triangles, and mixed through every warp: without the
-// queue half the lanes of a warp would idle through the front faces' work.
-// kDirect: compiled with the direct path (g.direct_max > 0), which needs more registers.
-template <bool kDirect>
+// A block takes tpb triangles, in chunks of setup_chunk(tpb), each in two phases.  Phase 1:
+// every triangle gets its sample range and the back-face proof (needs_setup); those with
+// nothing to rasterize store their range row and are done, the others are queued in
+// shared memory with their vertices and colour.  Phase 2: the queued triangles, dense in
+// the lanes, get the rest of their setup (setup_triangle) without touching global memory
+// for their inputs again.  Back faces are about half of a closed mesh's triangles, and
+// mixed through every warp: without the queue half the lanes of a warp would idle through
+// the front faces' work.  kDirect: compiled with the direct path (g.direct_max > 0), which
+// needs more registers.  kChunks: compiled for more than one chunk per block (tpb above
+// kSetupChunk); the one-chunk form keeps fewer values live through phase 2.
+template <bool kDirect, bool kChunks>
 __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFillMinBlocks)
 setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_base, FrameGeom g,
              FrameBuffers fb, BinBuffers bb, int tpb)
 {
-    __shared__ uint32_t squeue[kMaxTrianglesPerBlock];
     __shared__ uint32_t sq_n;
+    const uint32_t cap = (uint32_t)setup_chunk(tpb);
+    const SetupStash st{cap};
     if (threadIdx.x == 0) sq_n = 0;
     block_sync();
-    const uint32_t t0 = blockIdx.x * (uint32_t)tpb;
-    // two triangles per round, their vertex loads issued together
-    for (uint32_t t = t0 + threadIdx.x; t < t0 + (uint32_t)tpb; t += 2 * blockDim.x) {
-        const uint32_t u = t + blockDim.x;
-        const bool lt = t < mesh.ntri, lu = u < t0 + (uint32_t)tpb && u < mesh.ntri;
-        float4 a1, a2, a3, b1, b2, b3;
-        if (lt) triangle_vertices(mesh, tv, M, t, a1, a2, a3);
-        if (lu) triangle_vertices(mesh, tv, M, u, b1, b2, b3);
-        int4 row4;
-        const bool kt = lt && needs_setup(a1, a2, a3, g.w, g.h, row4);
-        if (lt && !kt) reinterpret_cast<int4 *>(fb.records + tri_base + t)[4] = row4;
-        const bool ku = lu && needs_setup(b1, b2, b3, g.w, g.h, row4);
-        if (lu && !ku) reinterpret_cast<int4 *>(fb.records + tri_base + u)[4] = row4;
-        queue_push(kt, t, squeue, &sq_n);
-        queue_push(ku, u, squeue, &sq_n);
-    }
-    block_sync();
-    const uint32_t nq = sq_n;
-    for (uint32_t base = 0; base < nq; base += blockDim.x) {
-        const uint32_t q = base + threadIdx.x;
-        setup_triangle<kDirect>(mesh, tv, M, tri_base, g, fb, bb, q < nq ? squeue[q] : 0xffffffffu);
+    const uint32_t t0 = blockIdx.x * (uint32_t)tpb, t_end = min(mesh.ntri, t0 + (uint32_t)tpb);
+    uint32_t base = 0;
+    for (uint32_t c0 = t0; c0 < t_end; c0 += cap) {
+        // two triangles per round, their vertex loads issued together (the trip count is
+        // the same in every lane: cap is a multiple of twice the block size or equals it)
+        for (uint32_t t = c0 + threadIdx.x; t < c0 + cap; t += 2 * blockDim.x) {
+            const uint32_t u = t + blockDim.x;
+            const bool lt = t < t_end, lu = u < c0 + cap && u < t_end;
+            float4 a1, a2, a3, b1, b2, b3;
+            uint32_t ca = 0, cb = 0;
+            if (lt) {
+                triangle_vertices(mesh, tv, M, t, a1, a2, a3);
+                ca = load_rgb(mesh.rgb, t);
+            }
+            if (lu) {
+                triangle_vertices(mesh, tv, M, u, b1, b2, b3);
+                cb = load_rgb(mesh.rgb, u);
+            }
+            int4 row4;
+            const bool kt = lt && needs_setup(a1, a2, a3, g.w, g.h, row4);
+            if (lt && !kt) reinterpret_cast<int4 *>(fb.records + tri_base + t)[4] = row4;
+            stash_push(st, &sq_n, base, kt, t, a1, a2, a3, ca);
+            const bool ku = lu && needs_setup(b1, b2, b3, g.w, g.h, row4);
+            if (lu && !ku) reinterpret_cast<int4 *>(fb.records + tri_base + u)[4] = row4;
+            stash_push(st, &sq_n, base, ku, u, b1, b2, b3, cb);
+        }
+        block_sync();
+        const uint32_t total = sq_n, nq = total - base;
+        for (uint32_t q0 = 0; q0 < nq; q0 += blockDim.x) {
+            const uint32_t q = q0 + threadIdx.x;
+            float4 p1, p2, p3;
+            uint32_t rgb = 0, t = 0;
+            if (q < nq) t = st.get(q, p1, p2, p3, rgb);
+            setup_triangle<kDirect>(tri_base, g, fb, bb, q < nq, t, p1, p2, p3, rgb);
+        }
+        if (!kChunks) break;
+        base = total;
+        if (c0 + cap < t_end) block_sync();   // the next chunk refills the stash
     }
 }
 
@@ -270,10 +288,16 @@ cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, u
     if (mesh.ntri == 0) return cudaSuccess;
     if (!valid_triangles_per_block(tpb)) return cudaErrorInvalidValue;
     const uint32_t blocks = (mesh.ntri + tpb - 1) / tpb;
-    if (g.direct_max > 0)
-        setup_kernel<true><<<blocks, setup_block_threads(tpb), 0, s>>>(mesh, tv, M, tri_base, g, fb, bb, tpb);
-    else
-        setup_kernel<false><<<blocks, setup_block_threads(tpb), 0, s>>>(mesh, tv, M, tri_base, g, fb, bb, tpb);
+    const size_t smem = setup_smem_bytes(tpb);   // at most 45,056 bytes: no opt-in needed
+    const dim3 grid(blocks), block(setup_block_threads(tpb));
+    const bool chunks = tpb > kSetupChunk;
+    if (g.direct_max > 0) {
+        if (chunks) setup_kernel<true, true><<<grid, block, smem, s>>>(mesh, tv, M, tri_base, g, fb, bb, tpb);
+        else setup_kernel<true, false><<<grid, block, smem, s>>>(mesh, tv, M, tri_base, g, fb, bb, tpb);
+    } else {
+        if (chunks) setup_kernel<false, true><<<grid, block, smem, s>>>(mesh, tv, M, tri_base, g, fb, bb, tpb);
+        else setup_kernel<false, false><<<grid, block, smem, s>>>(mesh, tv, M, tri_base, g, fb, bb, tpb);
+    }
     return cudaGetLastError();
 }
 

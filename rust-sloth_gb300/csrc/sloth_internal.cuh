@@ -29,19 +29,6 @@ __device__ __forceinline__ void block_sync()
     __syncthreads();
 }
 
-// Appends v to a shared-memory queue when keep holds, one shared atomic per warp (called
-// by all 32 lanes of the warp).
-__device__ __forceinline__ void queue_push(bool keep, uint32_t v, uint32_t *queue, uint32_t *count)
-{
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (!m) return;
-    const int lane = threadIdx.x & 31;
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(count, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (keep) queue[base + __popc(m & ((1u << lane) - 1u))] = v;
-}
-
 constexpr float kFltMax = 3.40282347e+38f;
 constexpr uint64_t kEmptyKey = ~0ull;
 constexpr uint32_t kSmallMaxTilesDev = 16;   // triangles over more tiles are binned by warps
@@ -75,18 +62,22 @@ __device__ __forceinline__ uint32_t shade_char(float s)
 //   edge 0: a = v2, b = v3   (w0 = orient(v2, v3, p))
 //   edge 1: a = v3, b = v1   (w1 = orient(v3, v1, p))
 //   edge 2: a = v1, b = v2   (w2 = orient(v1, v2, p))
+// Rows 0-1 (one 32-byte sector) hold all the resolve reads of a winning triangle in the
+// common case: the vertices' x and y (the edge deltas are their differences), the shade
+// factor and the colour.
 // ---------------------------------------------------------------------------------
 struct __align__(16) TriRecord {
     float v1x, v1y, v2x, v2y;       // row 0
-    float v3x, v3y, dx0, dy0;       // row 1
-    float dx1, dy1, dx2, dy2;       // row 2
-    float v1z, dz2, dz3, a;         // row 3: z = v1z + a*((w1*dz2) + (w2*dz3))
+    float v3x, v3y;                 // row 1
+    float na;                       //        normal().z * a (shade = na * ((w0+w1)+w2))
+    uint32_t rgb;                   //        r | g<<8 | b<<16
+    float dx0, dy0, dx1, dy1;       // row 2: dx0 = v3x - v2x, dx1 = v1x - v3x, dx2 = v2x - v1x
+    float dx2, dy2;                 // row 3
+    uint32_t flags;                 //        kFlag*
+    float zlo;                      //        lower bound of every depth the raster can compute
+                                    //        for this triangle, or -inf (bounds.cuh)
     int32_t x0, xe, y0, y1;         // row 4: sample rect [x0,xe) x [y0,y1) (xe: tight or loose)
-    float na;                       // row 5: normal().z * a (shade = na * ((w0+w1)+w2))
-    uint32_t rgb;                   // r | g<<8 | b<<16
-    uint32_t flags;                 // kFlag*
-    float zlo;                      // lower bound of every depth the raster can compute for
-                                    // this triangle, or -inf (bounds.cuh)
+    float v1z, dz2, dz3, a;         // row 5: z = v1z + a*((w1*dz2) + (w2*dz3))
 };
 static_assert(sizeof(TriRecord) == 96, "record layout");
 

@@ -121,6 +121,12 @@ constexpr int kTrianglesPerBlockChoices[4] = {128, 256, 1024, 4096};
 constexpr int kMaxTrianglesPerBlock = 4096;
 inline bool valid_triangles_per_block(long long v) { return v == 128 || v == 256 || v == 1024 || v == 4096; }
 __host__ __device__ inline int setup_block_threads(int tpb) { return tpb < kSetupThreads ? tpb : kSetupThreads; }
+// A setup block takes its triangles in chunks of at most kSetupChunk.  Phase 1 of a chunk
+// queues, in shared memory, the triangles that need the rest of their setup together with
+// their transformed vertices and colour (record.cuh: SetupStash, 44 bytes a triangle).
+constexpr int kSetupChunk = 1024;
+__host__ __device__ inline int setup_chunk(int tpb) { return tpb < kSetupChunk ? tpb : kSetupChunk; }
+__host__ __device__ inline size_t setup_smem_bytes(int tpb) { return 44u * (size_t)setup_chunk(tpb); }
 
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked
 // up once per device): grids of the grid-stride kernels are sized by it.
