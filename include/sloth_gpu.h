@@ -364,7 +364,7 @@ sloth_status sloth_batch_shade_backward(sloth_batch *batch, const float *vertex_
 #define SLOTH_NOALLOC_MAX_TRIANGLES 32768u
 #define SLOTH_NOALLOC_MAX_HEIGHT 4096u
 #define SLOTH_NOALLOC_MAX_DEPTH_CELLS 524288u
-#define SLOTH_NOALLOC_SCRATCH_BYTES 7508736u
+#define SLOTH_NOALLOC_SCRATCH_BYTES 7639808u
 sloth_status sloth_render_noalloc(const float *x, const float *y, const float *z, uint32_t ntri,
                                   const uint8_t *rgb, const float m[16], uint32_t width,
                                   uint32_t height, int image, uint32_t *cells, float *zbuf,

@@ -107,7 +107,7 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
     }
     // the smallest triangles fold their samples into the frame's global keys (direct.cuh)
     if (kDirect && __any_sync(0xffffffffu, direct)) {
-        const uint32_t frags = direct ? direct_raster(r, d.local_base + t, f.g.w, f.g.pitch,
+        const uint32_t frags = direct ? direct_raster(r, d.local_base + t, f.g.w, f.g.pitch, f.g.tw,
                                                       reinterpret_cast<unsigned long long *>(f.fb.keys), dw.xend,
                                                       dw.exit_mask)
                                       : 0u;
@@ -158,9 +158,11 @@ __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFi
             int4 row4;
             const bool kt = lt && needs_setup(a1, a2, a3, f.g.w, f.g.h, row4);
             if (lt && !kt) reinterpret_cast<int4 *>(f.fb.records + d.local_base + t)[4] = row4;
+            if (lt) f.fb.rows[d.local_base + t] = pack_rows(row4.z, row4.w);
             stash_push(st, &sq_n, base, kt, t, a1, a2, a3, ca);
             const bool ku = lu && needs_setup(b1, b2, b3, f.g.w, f.g.h, row4);
             if (lu && !ku) reinterpret_cast<int4 *>(f.fb.records + d.local_base + u)[4] = row4;
+            if (lu) f.fb.rows[d.local_base + u] = pack_rows(row4.z, row4.w);
             stash_push(st, &sq_n, base, ku, u, b1, b2, b3, cb);
         }
         block_sync();
@@ -196,8 +198,8 @@ __global__ void __launch_bounds__(1024) batch_newline_kernel(BatchDev b, const i
     const uint32_t lo = (uint32_t)blk.y, hi = min(d.mesh.ntri, lo + kBatchNewlineChunk);
     for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
         const int32_t v = (int32_t)(d.local_base + t);
-        const int4 yr = __ldg(reinterpret_cast<const int4 *>(f.fb.records + d.local_base + t) + 4);
-        nltree_update(tree, n, yr.z, yr.w, v, kShared);
+        const uint32_t yr = __ldg(f.fb.rows + d.local_base + t);
+        nltree_update(tree, n, (int)(yr & 0xffffu), (int)(yr >> 16), v, kShared);
     }
     if (kShared) {
         block_sync();
@@ -281,7 +283,7 @@ __global__ void __launch_bounds__(256) batch_items_kernel(BatchDev b)
             unsigned long long *k0 = reinterpret_cast<unsigned long long *>(f.fb.keys) +
                                      (size_t)tr * f.g.th * f.g.pitch + (size_t)tc * f.g.tw;
             for (int r = 0; r < f.g.th; ++r)
-                for (int c = 0; c < f.g.tw; ++c) k0[(size_t)r * f.g.pitch + c] = kEmptyKey;
+                for (int c = 0; c < live_keys_per_row(f.g.w, f.g.tw); ++c) k0[(size_t)r * f.g.pitch + c] = kEmptyKey;
             f.fb.tile_gen[lt] = f.fb.gen;
         }
     }

@@ -51,6 +51,7 @@ struct sloth_batch {
     Mat4 *h_mats = nullptr;                   // pinned
     float4 *tv = nullptr;
     TriRecord *records = nullptr;
+    uint32_t *rows = nullptr;                 // packed sample rows per record (setup -> newline)
     uint64_t *keys = nullptr;
     uint32_t *tile_gen = nullptr;
     int32_t *nltree = nullptr;
@@ -141,6 +142,7 @@ void free_layout(sloth_batch *b)
     bfree(b->d_mats);
     bfree(b->tv);
     bfree(b->records);
+    bfree(b->rows);
     bfree(b->keys);
     bfree(b->tile_gen);
     bfree(b->nltree);
@@ -266,6 +268,7 @@ sloth_status build(sloth_batch *b, int shape)
 
     BCU(b, balloc(&b->tv, vert));
     BCU(b, balloc(&b->records, rec));
+    BCU(b, balloc(&b->rows, rec));
     BCU(b, balloc(&b->keys, keys));
     BCU(b, balloc(&b->tile_gen, tiles));
     BCU(b, balloc(&b->nltree, nl));
@@ -293,6 +296,7 @@ sloth_status build(sloth_batch *b, int shape)
         bf.fb.tile_gen = b->tile_gen + tile_off[f];
         bf.fb.nltree = b->nltree + nl_off[f];
         bf.fb.records = b->records + rec_off[f];
+        bf.fb.rows = b->rows + rec_off[f];
         bf.fb.z_out = b->z + b->z_off[f];
         bf.fb.cells_out = b->cells + b->cell_off[f];
         bf.fb.winner_out = b->winner + b->z_off[f];

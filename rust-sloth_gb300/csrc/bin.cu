@@ -185,7 +185,7 @@ bin_items_kernel(uint32_t n, FrameGeom g, FrameBuffers fb, BinBuffers bb)
             unsigned long long *k0 = reinterpret_cast<unsigned long long *>(fb.keys) +
                                      (size_t)tr * g.th * g.pitch + (size_t)tc * g.tw;
             for (int r = 0; r < g.th; ++r)
-                for (int c = 0; c < g.tw; ++c) k0[(size_t)r * g.pitch + c] = kEmptyKey;
+                for (int c = 0; c < live_keys_per_row(g.w, g.tw); ++c) k0[(size_t)r * g.pitch + c] = kEmptyKey;
             fb.tile_gen[t] = fb.gen;
         }
         return;
@@ -200,7 +200,7 @@ bin_items_kernel(uint32_t n, FrameGeom g, FrameBuffers fb, BinBuffers bb)
         unsigned long long *k0 = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)tr * g.th * g.pitch +
                                  (size_t)tc * g.tw;
         for (int r = 0; r < g.th; ++r)
-            for (int c = 0; c < g.tw; ++c) k0[(size_t)r * g.pitch + c] = kEmptyKey;
+            for (int c = 0; c < live_keys_per_row(g.w, g.tw); ++c) k0[(size_t)r * g.pitch + c] = kEmptyKey;
         fb.tile_gen[t] = fb.gen;
     }
 }

@@ -29,14 +29,15 @@ __host__ __device__ __forceinline__ bool is_direct(int x0, int xe, int y0, int y
 // first column where an edge of exit_mask (bit i: edge i) is negative -- edges whose value
 // only falls along the row, so no later sample of the row can be covered.  Sample (x, y)
 // writes depth cell y*w + 2x (src/rasterizer.rs:80): row y, column 2x when 2x < w, else
-// row y+1, column 2x-w.  Returns the covered samples.
-__device__ __forceinline__ uint32_t direct_raster(const TriRecord &r, uint32_t gtri, int w, int pitch,
+// row y+1, column 2x-w, stored at key_col of its column for tile width tw.  Returns the
+// covered samples.
+__device__ __forceinline__ uint32_t direct_raster(const TriRecord &r, uint32_t gtri, int w, int pitch, int tw,
                                                  unsigned long long *keys, int xend, uint32_t exit_mask)
 {
     uint32_t frags = 0;
     for (int y = r.y0; y < r.y1; ++y) {
         const EdgeRows c = edge_rows(r, (float)y);
-        unsigned long long *rowu = keys + (size_t)y * pitch, *roww = rowu + pitch - w;
+        unsigned long long *rowu = keys + (size_t)y * pitch, *rown = rowu + pitch;
         for (int x = r.x0; x < xend; ++x) {
             const EdgeVals e = eval_edges_row(r, c, (float)x);
             const uint32_t neg = (e.w0 < 0.0f ? 1u : 0u) | (e.w1 < 0.0f ? 2u : 0u) | (e.w2 < 0.0f ? 4u : 0u);
@@ -47,7 +48,8 @@ __device__ __forceinline__ uint32_t direct_raster(const TriRecord &r, uint32_t g
                 if (z < kFltMax) {
                     // unwrapped: row y, column 2x; wrapped: row y+1, column 2x-w
                     const uint32_t nw = 2 * x < w ? 1u : 0u;
-                    red_min_u64((nw ? rowu : roww) + 2 * x, (unsigned long long)make_key(z, gtri, nw));
+                    red_min_u64((nw ? rowu : rown) + key_col(nw ? 2 * x : 2 * x - w, tw),
+                                (unsigned long long)make_key(z, gtri, nw));
                 }
             }
         }

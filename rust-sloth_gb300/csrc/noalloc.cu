@@ -14,6 +14,7 @@
 //
 // Scratch layout (byte offsets into g_noalloc_scratch):
 //   records   kMaxTri x 96 B          per-triangle setup records
+//   rows      kMaxTri x 4 B           per-triangle packed sample rows (setup -> newline)
 //   keys      kMaxCells x 8 B         depth keys (tiles padded to 64x32 cells)
 //   bins      tile counts/offsets/cursors, the large-triangle queue and its counter
 //   tile_gen  kMaxTiles x 4 B         tile generations (cleared every call)
@@ -33,7 +34,8 @@ constexpr uint32_t kMaxTiles = kMaxCells / (kTileW * kTileH);
 
 constexpr size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 constexpr size_t kOffRecords = 0;
-constexpr size_t kOffKeys = align256(kOffRecords + (size_t)kMaxTri * sizeof(TriRecord));
+constexpr size_t kOffRows = align256(kOffRecords + (size_t)kMaxTri * sizeof(TriRecord));
+constexpr size_t kOffKeys = align256(kOffRows + (size_t)kMaxTri * 4);
 constexpr size_t kOffCount = align256(kOffKeys + (size_t)kMaxCells * sizeof(uint64_t));
 constexpr size_t kOffOffset = align256(kOffCount + (size_t)kMaxTiles * 4);
 constexpr size_t kOffCursor = align256(kOffOffset + ((size_t)kMaxTiles + 1) * 4);
@@ -96,7 +98,7 @@ noalloc_raster_kernel(uint32_t ntri, FrameGeom g, FrameBuffers fb)
                         const unsigned long long key = make_key(z, t, nw);
                         const int row = nw ? (y - R0) : (y + 1 - R0);
                         const int col = nw ? (2 * x - C0) : (2 * x - g.w - C0);
-                        unsigned long long *p = &skeys[row * TW + col];
+                        unsigned long long *p = &skeys[row * TW + key_col(col, TW)];
                         if (key < *(volatile unsigned long long *)p) atomicMin(p, key);
                     }
                 }
@@ -108,6 +110,7 @@ noalloc_raster_kernel(uint32_t ntri, FrameGeom g, FrameBuffers fb)
     if (lane == 0) s_frags[threadIdx.x >> 5] = frags;
     block_sync();
     unsigned long long *gk = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)R0 * g.pitch + C0;
+    // shared and global keys share the layout (key_col): slot i of tile row rr is slot i globally
     for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
         const int rr = i / TW, cc = i - rr * TW;
         gk[(size_t)rr * g.pitch + cc] = skeys[i];
@@ -171,6 +174,7 @@ extern "C" sloth_status sloth_render_noalloc(const float *x, const float *y, con
 
     FrameBuffers fb{};
     fb.records = reinterpret_cast<TriRecord *>(base + kOffRecords);
+    fb.rows = reinterpret_cast<uint32_t *>(base + kOffRows);
     fb.keys = reinterpret_cast<uint64_t *>(base + kOffKeys);
     fb.tile_gen = reinterpret_cast<uint32_t *>(base + kOffGen);
     fb.nltree = reinterpret_cast<int32_t *>(base + kOffNl);

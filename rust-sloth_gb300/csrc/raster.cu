@@ -34,7 +34,8 @@ __device__ __forceinline__ void overflow_fold(uint32_t ntri, uint32_t tri_base, 
                 if (z < kFltMax) {
                     const uint32_t nw = 2 * x < g.w ? 1u : 0u;
                     const int row = nw ? y : y + 1, col = nw ? 2 * x : 2 * x - g.w;
-                    red_min_u64(keys + (size_t)row * g.pitch + col, (unsigned long long)make_key(z, gtri, nw));
+                    red_min_u64(keys + (size_t)row * g.pitch + key_col(col, g.tw),
+                                (unsigned long long)make_key(z, gtri, nw));
                 }
             }
         }

@@ -129,7 +129,7 @@ __device__ __forceinline__ void fold_sample(const TriRecord &r, uint32_t gtri, i
 {
     const int row = kNotWrapped ? (y - R0) : (y + 1 - R0);
     const int col = kNotWrapped ? (2 * x - C0) : (2 * x - w - C0);
-    unsigned long long *p = &skeys[row * TW + col];
+    unsigned long long *p = &skeys[row * TW + key_col(col, TW)];
     if (zb > *(volatile const uint32_t *)(reinterpret_cast<const uint32_t *>(p) + 1)) return;
     // with the row's edge terms given (a walk along one row), only the column terms remain
     const EdgeVals e = rows ? eval_edges_row(r, *rows, (float)x) : eval_edges(r, (float)x, (float)y);
@@ -279,43 +279,58 @@ constexpr int kSerialWideSamples = 16;
 // word) among the tile's cells that unwrapped samples can write (row y in [1,h-2], column
 // 2x in [2,w-1], even) and among those wrapped samples can write (row y+1 in [2,h-1],
 // column 2x-w in [0,w-4], of the parity of w); rmu[i] / rmw[i] are the same over tile row
-// i.  Lane i of the refreshing warp reads row i (16-byte reads of (even, odd) cell pairs,
-// rotated by lane so that the lanes of a read hit different banks) and folds its maxima in
-// with atomicMin.  Reads race with the atomics of other warps; key values only decrease,
-// so every bound read stays an upper bound of every later state.
+// i.  Lane i of the refreshing warp reads row i: 16-byte reads of two keys of the row's
+// even half (columns 4j and 4j+2), and of its odd half (4j+1, 4j+3) when w is odd, rotated
+// by lane so that the lanes of a read hit different banks; it folds its maxima in with
+// atomicMin.  Reads race with the atomics of other warps; key values only decrease, so
+// every bound read stays an upper bound of every later state.
+__device__ __forceinline__ void ld_hi2(uint32_t addr, uint32_t &hi0, uint32_t &hi1)
+{
+    uint32_t lo0, lo1;
+    asm volatile("ld.volatile.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(lo0), "=r"(hi0), "=r"(lo1), "=r"(hi1)
+                 : "r"(addr));
+}
+
 template <int TW, int TH>
 __device__ __forceinline__ void refresh_bounds(TileSmem<TW, TH> &S, int R0, int C0, const FrameGeom &g, int lane)
 {
-    constexpr int P = TW / 2;   // cell pairs per row
-    static_assert((P & (P - 1)) == 0, "rotation by mask");
+    constexpr int Q = TW / 4;   // 16-byte reads per half row
+    static_assert((Q & (Q - 1)) == 0, "rotation by mask");
     const int wpar = g.w & 1;
     uint32_t mu = 0, mw = 0;
     if (lane < TH) {
-        const uint32_t base = smem_u32(S.keys) + 8u * (uint32_t)(lane * TW);
+        const uint32_t even = smem_u32(S.keys) + 8u * (uint32_t)(lane * TW), odd = even + 4u * (uint32_t)TW;
         if (R0 >= 2 && R0 + TH <= g.h - 1 && C0 >= 2 && C0 + TW <= g.w - 3) {
             // every cell of the tile is writable: unwrapped samples write the even columns,
             // wrapped ones the columns of w's parity (C0 is even)
 #pragma unroll 8
-            for (int k = 0; k < P; ++k) {
-                uint32_t lo0, hi0, lo1, hi1;
-                asm volatile("ld.volatile.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
-                             : "=r"(lo0), "=r"(hi0), "=r"(lo1), "=r"(hi1)
-                             : "r"(base + 16u * (uint32_t)((k + lane) & (P - 1))));
-                mu = max(mu, hi0);
-                mw = max(mw, wpar ? hi1 : hi0);
+            for (int k = 0; k < Q; ++k) {
+                const uint32_t off = 16u * (uint32_t)((k + lane) & (Q - 1));
+                uint32_t h0, h1;
+                ld_hi2(even + off, h0, h1);
+                mu = max(mu, max(h0, h1));
+                if (wpar) {
+                    ld_hi2(odd + off, h0, h1);
+                    mw = max(mw, max(h0, h1));
+                }
             }
+            if (!wpar) mw = mu;
         } else {
             const int gr = R0 + lane;
             const bool ru = gr >= 1 && gr <= g.h - 2, rw = gr >= 2 && gr <= g.h - 1;
-            for (int k = 0; k < P; ++k) {
-                const int pi = (k + lane) & (P - 1);
-                uint32_t lo0, hi0, lo1, hi1;
-                asm volatile("ld.volatile.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
-                             : "=r"(lo0), "=r"(hi0), "=r"(lo1), "=r"(hi1)
-                             : "r"(base + 16u * (uint32_t)pi));
-                const int gc = C0 + 2 * pi;   // even
-                if (ru && gc >= 2 && gc <= g.w - 1) mu = max(mu, hi0);
-                if (rw && gc + wpar <= g.w - 4) mw = max(mw, wpar ? hi1 : hi0);
+            for (int k = 0; k < Q; ++k) {
+                const int j = (k + lane) & (Q - 1);
+                const int gc = C0 + 4 * j;   // columns gc, gc + 2 (even); gc + 1, gc + 3 (odd)
+                uint32_t h0, h1;
+                ld_hi2(even + 16u * (uint32_t)j, h0, h1);
+                if (ru && gc >= 2 && gc <= g.w - 1) mu = max(mu, h0);
+                if (ru && gc + 2 >= 2 && gc + 2 <= g.w - 1) mu = max(mu, h1);
+                if (rw) {
+                    if (wpar) ld_hi2(odd + 16u * (uint32_t)j, h0, h1);
+                    if (gc + wpar <= g.w - 4) mw = max(mw, h0);
+                    if (gc + 2 + wpar <= g.w - 4) mw = max(mw, h1);
+                }
             }
         }
         atomicMin(&S.rmu[lane], mu);
@@ -351,8 +366,9 @@ __device__ __forceinline__ bool raster_tile(TileSmem<TW, TH> &S, const FrameGeom
     const int R0 = tr * TH, C0 = tc * TW;
     const bool merge = !split && fb.tile_gen[tile] == fb.gen;
     unsigned long long *gk = reinterpret_cast<unsigned long long *>(fb.keys) + (size_t)R0 * g.pitch + C0;
+    const int live = live_keys_per_row(g.w, TW);   // keys of a tile row that samples can write
     if (merge) {
-        // keys of earlier draws since the clear: one bulk copy per tile row (TW*8 bytes,
+        // keys of earlier draws since the clear: one bulk copy per tile row (live*8 bytes,
         // 16-byte aligned at both ends), completing on an mbarrier
         if (threadIdx.x < 32) {
             // warp 0: lane 0 arms the barrier for this phase, then the lanes issue one row each
@@ -361,11 +377,11 @@ __device__ __forceinline__ bool raster_tile(TileSmem<TW, TH> &S, const FrameGeom
                     mbar_init(&S.kbar, 1);
                     fence_proxy_async_smem();
                 }
-                mbar_expect_tx(&S.kbar, (uint32_t)(TH * TW * sizeof(unsigned long long)) + (fb.wait_test ? 16u : 0u));
+                mbar_expect_tx(&S.kbar, (uint32_t)(TH * live * sizeof(unsigned long long)) + (fb.wait_test ? 16u : 0u));
             }
             __syncwarp();
             for (int rr = threadIdx.x; rr < TH; rr += 32)
-                bulk_load(&S.keys[rr * TW], gk + (size_t)rr * g.pitch, TW * sizeof(unsigned long long), &S.kbar);
+                bulk_load(&S.keys[rr * TW], gk + (size_t)rr * g.pitch, live * sizeof(unsigned long long), &S.kbar);
         }
         block_sync();
         if (threadIdx.x == 0) {
@@ -380,7 +396,8 @@ __device__ __forceinline__ bool raster_tile(TileSmem<TW, TH> &S, const FrameGeom
             return false;
         }
     } else {
-        for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) S.keys[i] = kEmptyKey;
+        for (int i = threadIdx.x; i < TH * TW; i += blockDim.x)
+            if ((i & (TW - 1)) < live) S.keys[i] = kEmptyKey;
     }
     if (threadIdx.x == 0) S.zmax_u = S.zmax_w = 0xffffffffu;
     if (threadIdx.x < 64) (threadIdx.x < 32 ? S.rmu : S.rmw)[threadIdx.x & 31] = 0xffffffffu;
@@ -568,13 +585,14 @@ __device__ __forceinline__ bool raster_tile(TileSmem<TW, TH> &S, const FrameGeom
         if (threadIdx.x < 32) {
             // warp 0: one row per lane, each lane waits for its own copies
             for (int rr = threadIdx.x; rr < TH; rr += 32)
-                bulk_store(gk + (size_t)rr * g.pitch, &S.keys[rr * TW], TW * sizeof(unsigned long long));
+                bulk_store(gk + (size_t)rr * g.pitch, &S.keys[rr * TW], live * sizeof(unsigned long long));
             bulk_store_drain();
         }
     } else {
+        // shared and global keys share the layout: slot i of tile row rr is slot i globally
         for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
             const int rr = i / TW, cc = i - rr * TW;
-            if (S.keys[i] != kEmptyKey) red_min_u64(&gk[(size_t)rr * g.pitch + cc], S.keys[i]);
+            if (cc < live && S.keys[i] != kEmptyKey) red_min_u64(&gk[(size_t)rr * g.pitch + cc], S.keys[i]);
         }
     }
     if (threadIdx.x < 32) {

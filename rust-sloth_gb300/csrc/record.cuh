@@ -94,7 +94,8 @@ __device__ __forceinline__ void store_record(TriRecord *dst, const TriRecord &r,
 // rest of their setup: the sample range and the back-face proof over the untightened range
 // (the same operations as build_record).  Returns false for a triangle with an empty range
 // or proven to cover no sample, with `row4` its record row 4 (x0, xe, y0, y1) -- all that
-// is ever read of such a triangle; true when the triangle needs build_record.
+// is ever read of such a triangle; true when the triangle needs build_record.  Either way
+// row4.z and row4.w are the rows [y0, y1) the record will hold.
 __device__ __forceinline__ bool needs_setup(float4 p1, float4 p2, float4 p3, int w, int h, int4 &row4)
 {
     TriRecord r;   // the fields orient_bound reads
@@ -120,8 +121,13 @@ __device__ __forceinline__ bool needs_setup(float4 p1, float4 p2, float4 p3, int
         row4 = make_int4(r.x0, r.x0, r.y0, r.y1);
         return false;
     }
+    row4 = make_int4(r.x0, x1, r.y0, r.y1);
     return true;
 }
+
+// A triangle's sample rows [y0, y1) packed for the newline kernels (FrameBuffers::rows):
+// both lie in [0, h] and h is at most 65535.
+__device__ __forceinline__ uint32_t pack_rows(int y0, int y1) { return (uint32_t)y0 | ((uint32_t)y1 << 16); }
 
 // Face colour of triangle t: three bytes, packed as the record stores them.
 __device__ __forceinline__ uint32_t load_rgb(const uint8_t *rgb, uint32_t t)

@@ -34,11 +34,14 @@ __device__ __forceinline__ bool later(const Cand &a, const Cand &b)
 
 __device__ __forceinline__ uint64_t key_at(const FrameGeom &g, const FrameBuffers &fb, int r, int cc)
 {
+    // no sample writes an odd column of an even-width frame, and its key is not kept
+    if (!(g.w & 1) && (cc & 1)) return kEmptyKey;
     // tile sides are powers of two; both reads issued before either is tested (the key
     // of a tile of an older generation is in bounds, only stale)
     const int tile = (r >> (__ffs(g.th) - 1)) * g.ntx + (cc >> (__ffs(g.tw) - 1));
     const uint32_t gen = __ldg(fb.tile_gen + tile);
-    const uint64_t k = __ldg(reinterpret_cast<const unsigned long long *>(fb.keys) + (size_t)r * g.pitch + cc);
+    const uint64_t k =
+        __ldg(reinterpret_cast<const unsigned long long *>(fb.keys) + (size_t)r * g.pitch + key_col(cc, g.tw));
     return gen == fb.gen ? k : kEmptyKey;
 }
 

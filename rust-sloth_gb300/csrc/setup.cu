@@ -110,7 +110,7 @@ __device__ __forceinline__ void setup_triangle(uint32_t tri_base, const FrameGeo
     }
     // the smallest triangles fold their samples into the global keys here (direct.cuh)
     if (kDirect && __any_sync(0xffffffffu, direct)) {
-        const uint32_t frags = direct ? direct_raster(r, tri_base + t, g.w, g.pitch,
+        const uint32_t frags = direct ? direct_raster(r, tri_base + t, g.w, g.pitch, g.tw,
                                                       reinterpret_cast<unsigned long long *>(fb.keys), dw.xend,
                                                       dw.exit_mask)
                                       : 0u;
@@ -159,9 +159,11 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
             int4 row4;
             const bool kt = lt && needs_setup(a1, a2, a3, g.w, g.h, row4);
             if (lt && !kt) reinterpret_cast<int4 *>(fb.records + tri_base + t)[4] = row4;
+            if (lt) fb.rows[tri_base + t] = pack_rows(row4.z, row4.w);
             stash_push(st, &sq_n, base, kt, t, a1, a2, a3, ca);
             const bool ku = lu && needs_setup(b1, b2, b3, g.w, g.h, row4);
             if (lu && !ku) reinterpret_cast<int4 *>(fb.records + tri_base + u)[4] = row4;
+            if (lu) fb.rows[tri_base + u] = pack_rows(row4.z, row4.w);
             stash_push(st, &sq_n, base, ku, u, b1, b2, b3, cb);
         }
         block_sync();
@@ -185,7 +187,8 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
 // [y0,y1) contains y.  Each triangle folds its interval into a max segment tree with
 // O(log h) node updates (canonical decomposition); a row's value is the maximum over its
 // leaf-to-root path.  Each block builds a tree for a chunk of triangles in shared memory,
-// then merges its non-empty nodes into the frame's tree.
+// then merges its non-empty nodes into the frame's tree.  The rows come from the packed
+// array setup wrote (4 bytes a triangle, read in order), not from the records' row 4.
 template <bool kShared>
 __global__ void __launch_bounds__(1024)
 newline_kernel(uint32_t ntri, uint32_t tri_base, uint32_t chunk, FrameGeom g, FrameBuffers fb)
@@ -200,8 +203,8 @@ newline_kernel(uint32_t ntri, uint32_t tri_base, uint32_t chunk, FrameGeom g, Fr
     const uint32_t lo = blockIdx.x * chunk, hi = min(ntri, lo + chunk);
     for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
         const int32_t v = (int32_t)(tri_base + t);
-        const int4 yr = __ldg(reinterpret_cast<const int4 *>(fb.records + tri_base + t) + 4);
-        nltree_update(tree, n, yr.z, yr.w, v, kShared);
+        const uint32_t yr = __ldg(fb.rows + tri_base + t);
+        nltree_update(tree, n, (int)(yr & 0xffffu), (int)(yr >> 16), v, kShared);
     }
     if (kShared) {
         block_sync();

@@ -245,14 +245,18 @@ static sloth_status ensure_records(sloth_ctx *ctx, size_t need)
     size_t cap = ctx->records_cap ? ctx->records_cap : 1024;
     while (cap < need) cap *= 2;
     TriRecord *n = nullptr;
+    uint32_t *rows = nullptr;
     CU(ctx, dalloc(&n, cap));
+    CU(ctx, dalloc(&rows, cap));   // read only by the newline fold of the draw that wrote them
     if (ctx->fb.records && ctx->tri_base)
         CU(ctx, cudaMemcpyAsync(n, ctx->fb.records, (size_t)ctx->tri_base * sizeof(TriRecord),
                                 cudaMemcpyDeviceToDevice, ctx->stream));
     CU(ctx, cudaStreamSynchronize(ctx->stream));
     quiesce_helpers(ctx);
     dfree(ctx->fb.records);
+    dfree(ctx->fb.rows);
     ctx->fb.records = n;
+    ctx->fb.rows = rows;
     ctx->records_cap = cap;
     return SLOTH_OK;
 }
@@ -521,6 +525,7 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
         }
     free_frame(ctx);
     dfree(ctx->fb.records);
+    dfree(ctx->fb.rows);
     dfree(ctx->bb.entries);
     dfree(ctx->bb.large_queue);
     dfree(ctx->bb.large_count);

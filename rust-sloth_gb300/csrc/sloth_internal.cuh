@@ -156,7 +156,20 @@ __device__ __forceinline__ uint64_t make_key(float z, uint32_t tri, uint32_t not
 // Target-cell tiling.  Sample (x,y) writes depth cell id = y*w + 2x (src/rasterizer.rs:80):
 // row y, column 2x when 2x < w ("unwrapped"), else row y+1, column 2x-w ("wrapped").
 // Tiles partition depth cells; every writer of a cell lands in the cell's tile.
+//
+// Key layout.  Within every aligned run of tw cells of a row (a tile row) the keys of the
+// even columns come first, then those of the odd columns: column c is stored at key_col(c).
+// Unwrapped samples write even columns, wrapped ones columns of w's parity, so when w is
+// even only the first half of each tile row is ever written (its other half is neither
+// copied, cleared nor read), and a warp's samples along a row hit consecutive keys.
 // ---------------------------------------------------------------------------------
+__host__ __device__ __forceinline__ int key_col(int c, int tw)
+{
+    return (c & ~(tw - 1)) | ((c & 1) ? (tw >> 1) : 0) | ((c & (tw - 1)) >> 1);
+}
+// Keys of one tile row that are ever written: half of them when w is even.
+__host__ __device__ __forceinline__ int live_keys_per_row(int w, int tw) { return (w & 1) ? tw : tw >> 1; }
+
 struct Viewport {
     int32_t w, h;           // sample grid / depth cells
     int32_t image;

@@ -29,6 +29,7 @@ struct FrameBuffers {
     int32_t *nltree;         // 2*nl_size: max segment tree over rows of the draw indices whose
                              // newline row range [y0,y1) covers each node (-1 = none)
     TriRecord *records;      // draw index -> record
+    uint32_t *rows;          // draw index -> sample rows y0 | y1 << 16 (setup writes, the newline reads)
     float *z_out;            // w*h
     uint32_t *cells_out;     // w*h (+h)
     int32_t *winner_out;     // w*h
