@@ -4,13 +4,21 @@
 
 namespace sloth {
 
-// Runs of kRun frame cells; each warp takes 32 consecutive runs (resolve_run).
+// Runs of kRun frame cells; each warp takes 32 consecutive runs (resolve_run).  An
+// even-width frame goes by pairs of cells instead, kEvenPairs per thread (resolve_even).
 constexpr int kRun = 2;
+constexpr int kEvenPairs = 4;
 
 __global__ void __launch_bounds__(256) resolve_kernel(FrameGeom g, FrameBuffers fb, int vec)
 {
     const uint64_t nz = (uint64_t)g.w * g.h;
     const uint64_t ncells = g.image ? nz + g.h : nz;
+    if (!(g.w & 1)) {
+        const uint64_t npairs = (ncells + 1) / 2, span = (uint64_t)blockDim.x * kEvenPairs;
+        for (uint64_t base = blockIdx.x * span; base < npairs; base += (uint64_t)gridDim.x * span)
+            resolve_even<kEvenPairs>(g, fb, base + threadIdx.x, blockDim.x, npairs, vec != 0);
+        return;
+    }
     const uint64_t nruns = (ncells + kRun - 1) / kRun;
     const int lane = threadIdx.x & 31;
     for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < nruns; base += (uint64_t)gridDim.x * blockDim.x) {
@@ -23,7 +31,8 @@ cudaError_t launch_resolve(const FrameGeom &g, const FrameBuffers &fb, cudaStrea
 {
     const uint64_t ncells = (uint64_t)g.w * g.h + (g.image ? g.h : 0);
     if (ncells == 0) return cudaSuccess;
-    uint64_t blocks = ((ncells + kRun - 1) / kRun + 255) / 256;
+    const uint64_t per_block = 256ull * kRun * ((g.w & 1) ? 1 : kEvenPairs);   // cells
+    uint64_t blocks = (ncells + per_block - 1) / per_block;
     const uint64_t cap = 32ull * (uint64_t)device_sm_count();   // eight resident CTAs per SM, four waves
     if (blocks > cap) blocks = cap;
     const int vec = ((reinterpret_cast<uintptr_t>(fb.cells_out) | reinterpret_cast<uintptr_t>(fb.z_out) |

@@ -45,9 +45,9 @@ __device__ __forceinline__ uint64_t key_at(const FrameGeom &g, const FrameBuffer
     return gen == fb.gen ? k : kEmptyKey;
 }
 
-// Rebuild the winning write of depth cell (r, cc) from its key.
-__device__ __forceinline__ Cand decode(const FrameGeom &g, const FrameBuffers &fb, uint64_t key,
-                                       int r, int cc, float *z_out)
+// decode() with the winner's record rows 0-1 already loaded (q0, q1).
+__device__ __forceinline__ Cand decode_rows(const FrameGeom &g, const FrameBuffers &fb, uint64_t key, int r, int cc,
+                                            float4 q0, float4 q1, float *z_out)
 {
     Cand c;
     const uint32_t lo = (uint32_t)key;
@@ -61,8 +61,6 @@ __device__ __forceinline__ Cand decode(const FrameGeom &g, const FrameBuffers &f
     }
     // rows 0-1 (one 32-byte sector): vertices, shade factor, colour; the edge deltas are
     // the subtractions setup made (build_record)
-    const float4 *p = reinterpret_cast<const float4 *>(fb.records + c.tri);
-    const float4 q0 = __ldg(p), q1 = __ldg(p + 1);
     TriRecord rec;
     rec.v1x = q0.x; rec.v1y = q0.y; rec.v2x = q0.z; rec.v2y = q0.w; rec.v3x = q1.x; rec.v3y = q1.y;
     rec.dx0 = fsub(rec.v3x, rec.v2x); rec.dy0 = fsub(rec.v3y, rec.v2y);
@@ -77,12 +75,20 @@ __device__ __forceinline__ Cand decode(const FrameGeom &g, const FrameBuffers &f
         if (hi != ordered_z(0.0f)) {
             *z_out = float_of_ordered(hi);
         } else {
-            const float4 q5 = __ldg(p + 5);
+            const float4 q5 = __ldg(reinterpret_cast<const float4 *>(fb.records + c.tri) + 5);
             *z_out = interp_z(q5.x, q5.y, q5.z, q5.w, e.w1, e.w2);
         }
     }
     c.cell = shade_char(shade) | (__float_as_uint(q1.w) << 8);
     return c;
+}
+
+// Rebuild the winning write of depth cell (r, cc) from its key.
+__device__ __forceinline__ Cand decode(const FrameGeom &g, const FrameBuffers &fb, uint64_t key,
+                                       int r, int cc, float *z_out)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(fb.records + ((uint32_t)key >> 1));
+    return decode_rows(g, fb, key, r, cc, __ldg(p), __ldg(p + 1), z_out);
 }
 
 // Resolve frame cell c (and depth cell c when c < w*h) of one frame.
@@ -361,6 +367,84 @@ __device__ __forceinline__ void resolve_run(const FrameGeom &g, const FrameBuffe
                 fb.z_out[c0 + j] = z[j];
                 fb.winner_out[c0 + j] = hc[j] ? (int32_t)kc[j].tri : -1;
             }
+    }
+}
+
+// Resolve of an even-width frame, pairs of frame cells (c0 = 2p, c0+1).  Samples write
+// only even depth columns there (y*w + 2x is even), so depth cell c0+1 never has a winner:
+// frame cell c0 takes the winner of depth cell c0 (its left neighbour c0-1 is odd and the
+// newline cells y*w+1 are odd), and frame cell c0+1 the later of that winner and, when c0
+// starts a row, the row's newline (the rule of resolve_cell).  A thread resolves the J
+// pairs p0 + j*stride below pend, issuing every key load first, then every winner's record
+// loads, then the arithmetic and stores: J independent chains in flight instead of one.
+// With vec the outputs are 8-byte aligned and a pair goes out in one store per buffer.
+template <int J>
+__device__ __forceinline__ void resolve_even(const FrameGeom &g, const FrameBuffers &fb, uint64_t p0, uint32_t stride,
+                                             uint64_t pend, bool vec)
+{
+    const uint64_t nz = (uint64_t)g.w * g.h;
+    const uint64_t ncells = g.image ? nz + g.h : nz;
+    uint64_t key[J];
+    int rr[J], cc[J];
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+        const uint64_t c0 = 2 * (p0 + (uint64_t)j * stride);
+        key[j] = kEmptyKey;
+        rr[j] = 0;
+        cc[j] = 0;
+        if (c0 < nz) {
+            rr[j] = nz <= 0xffffffffull ? (int)((uint32_t)c0 / (uint32_t)g.w) : (int)(c0 / (uint64_t)g.w);
+            cc[j] = (int)(c0 - (uint64_t)rr[j] * g.w);
+            key[j] = key_at(g, fb, rr[j], cc[j]);
+        }
+    }
+    float4 q0[J], q1[J];
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+        q0[j] = q1[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (key[j] != kEmptyKey) {
+            const float4 *rp = reinterpret_cast<const float4 *>(fb.records + ((uint32_t)key[j] >> 1));
+            q0[j] = __ldg(rp);
+            q1[j] = __ldg(rp + 1);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+        const uint64_t p = p0 + (uint64_t)j * stride;
+        if (p >= pend) continue;
+        const uint64_t c0 = 2 * p;
+        const bool have = key[j] != kEmptyKey;
+        float z = kFltMax;
+        Cand best{0, 0, 0, (uint32_t)' '};
+        if (have) best = decode_rows(g, fb, key[j], rr[j], cc[j], q0[j], q1[j], &z);
+        const uint32_t out0 = best.cell;
+        // frame cell c0+1: depth cell c0's winner, or the newline of row rr when c0 starts it
+        uint32_t out1 = best.cell;
+        if (g.image && c0 < nz && cc[j] == 0) {
+            const int32_t t = nltree_query(fb.nltree, g.nl_size, rr[j]);
+            if (t >= 0) {
+                const Cand n{(uint32_t)t, rr[j], INT_MAX, (uint32_t)'\n'};
+                if (!have || later(n, best)) out1 = n.cell;
+            }
+        }
+        if (vec && c0 + 2 <= ncells) {
+            *reinterpret_cast<uint2 *>(fb.cells_out + c0) = make_uint2(out0, out1);
+        } else {
+            fb.cells_out[c0] = out0;
+            if (c0 + 1 < ncells) fb.cells_out[c0 + 1] = out1;
+        }
+        if (c0 < nz) {   // nz is even: c0 + 1 < nz too
+            const int32_t w0 = have ? (int32_t)best.tri : -1;
+            if (vec) {
+                *reinterpret_cast<float2 *>(fb.z_out + c0) = make_float2(z, kFltMax);
+                *reinterpret_cast<int2 *>(fb.winner_out + c0) = make_int2(w0, -1);
+            } else {
+                fb.z_out[c0] = z;
+                fb.z_out[c0 + 1] = kFltMax;
+                fb.winner_out[c0] = w0;
+                fb.winner_out[c0 + 1] = -1;
+            }
+        }
     }
 }
 
