@@ -73,7 +73,7 @@ __device__ __forceinline__ void batch_triangle_vertices(const BatchDev &b, const
 template <bool kDirect>
 __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const BatchDraw &d, const BatchFrame &f,
                                                      bool live, uint32_t t, float4 p1, float4 p2, float4 p3,
-                                                     uint32_t rgb)
+                                                     uint32_t rgb, uint32_t stage)
 {
     bool large = false, direct = false;
     DirectWalk dw{false, 0, 0u};
@@ -107,10 +107,9 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
     }
     // the smallest triangles fold their samples into the frame's global keys (direct.cuh)
     if (kDirect && __any_sync(0xffffffffu, direct)) {
-        const uint32_t frags = direct ? direct_raster(r, d.local_base + t, f.g.w, f.g.pitch, f.g.tw,
-                                                      reinterpret_cast<unsigned long long *>(f.fb.keys), dw.xend,
-                                                      dw.exit_mask)
-                                      : 0u;
+        const uint32_t frags = direct_raster_warp(direct, r, d.local_base + t, f.g.w, f.g.pitch, f.g.tw,
+                                                  reinterpret_cast<unsigned long long *>(f.fb.keys), dw.xend,
+                                                  dw.exit_mask, stage);
         add_frags_warp(frags, f.fb.fragments);
     }
 }
@@ -172,7 +171,8 @@ __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFi
             float4 p1, p2, p3;
             uint32_t rgb = 0, t = 0;
             if (q < nq) t = st.get(q, p1, p2, p3, rgb);
-            batch_setup_triangle<kDirect>(b, d, f, q < nq, t, p1, p2, p3, rgb);
+            batch_setup_triangle<kDirect>(b, d, f, q < nq, t, p1, p2, p3, rgb,
+                                          11u * cap + (threadIdx.x >> 5) * (uint32_t)kDirectStageWords);
         }
         if (!kChunks) break;
         base = total;
@@ -368,6 +368,11 @@ __global__ void __launch_bounds__(256) batch_resolve_kernel(BatchDev b, const in
 
 cudaError_t prepare_batch_kernels()
 {
+    const int bytes = (int)setup_smem_bytes(kMaxTrianglesPerBlock, true);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(batch_setup_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) ||
+        (e = cudaFuncSetAttribute(batch_setup_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
     return cudaFuncSetAttribute(batch_newline_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 128 * 1024);
 }
@@ -383,7 +388,7 @@ cudaError_t launch_batch_setup(const BatchDev &b, const int2 *blocks, uint32_t n
 {
     if (!nblocks) return cudaSuccess;
     if (!valid_triangles_per_block(b.tpb)) return cudaErrorInvalidValue;
-    const size_t smem = setup_smem_bytes(b.tpb);   // at most 45,056 bytes: no opt-in needed
+    const size_t smem = setup_smem_bytes(b.tpb, b.direct_max > 0);   // prepare_batch_kernels: above 48 KB
     const dim3 grid(nblocks), block(setup_block_threads(b.tpb));
     const bool chunks = b.tpb > kSetupChunk;
     if (b.direct_max > 0) {

@@ -14,6 +14,8 @@
 // empty key) before the first direct fold of a frame.
 #pragma once
 
+#include <climits>
+
 #include "sloth_internal.cuh"
 
 namespace sloth {
@@ -54,6 +56,118 @@ __device__ __forceinline__ uint32_t direct_raster(const TriRecord &r, uint32_t g
             }
         }
     }
+    return frags;
+}
+
+// The direct triangles of a warp folded together (called by all 32 lanes; lanes with
+// mine false bring none).  Each triangle's samples are its rows [y0, y1) times the columns
+// [x0, xs): xs = xend for a triangle walked over its stored range (exit_mask 0); with row
+// exits, xs = min(r.xe + 1, xend), the unproven end plus one probe column.  The warp walks
+// the concatenation of all its triangles' samples 32 at a time, each lane finding its
+// triangle by a binary search over the running ends, so that the lanes stay busy and one
+// reduction instruction covers neighbouring samples of a few triangles (fewer memory
+// requests).  A covered sample is never past a row's exit (an exit edge, once negative,
+// stays negative along the row), so walking every column up to the probe folds the same
+// samples as the row walk of direct_raster.  When the probe column still has no exit edge
+// negative, the lane that tested it walks the rest of that row as direct_raster does.
+// The warp stages its triangles in kDirectStageWords words of the setup kernels' dynamic
+// shared memory from word `stage` on (structure of arrays: field f of lane l at f*32 + l,
+// so lanes reading one triangle share a broadcast and different triangles fall in
+// different banks).
+constexpr int kDirectFields = 23;
+constexpr int kDirectStageWords = kDirectFields * 32;
+
+// The setup kernels' dynamic shared memory (record.cuh: SetupStash; then one direct stage
+// per warp).  Indexing the array itself keeps the accesses 32-bit shared ones.
+extern __shared__ uint32_t setup_smem[];
+
+__device__ __forceinline__ uint32_t direct_raster_warp(bool mine, const TriRecord &r, uint32_t gtri, int w, int pitch,
+                                                      int tw, unsigned long long *keys, int xend, uint32_t exit_mask,
+                                                      uint32_t stage)
+{
+    const int lane = threadIdx.x & 31;
+    float *sf = reinterpret_cast<float *>(setup_smem + stage);
+    int *si = reinterpret_cast<int *>(setup_smem + stage);
+    int n = 0;
+    if (mine) {
+        const bool probe = exit_mask != 0u && r.xe < xend;   // r.xe <= xend always
+        const int xs = probe ? r.xe + 1 : xend;
+        const int cols = xs - r.x0;
+        n = cols * (r.y1 - r.y0);
+        const float v[16] = {r.v1x, r.v1y, r.v2x, r.v2y, r.v3x, r.v3y, r.dx0, r.dy0,
+                             r.dx1, r.dy1, r.dx2, r.dy2, r.v1z, r.dz2, r.dz3, r.a};
+#pragma unroll
+        for (int f = 0; f < 16; ++f) sf[f * 32 + lane] = v[f];
+        si[16 * 32 + lane] = r.x0;
+        si[17 * 32 + lane] = r.y0;
+        si[18 * 32 + lane] = cols;
+        si[19 * 32 + lane] = probe ? r.xe : INT_MAX;
+        si[20 * 32 + lane] = xend;
+        si[21 * 32 + lane] = (int)exit_mask;
+        si[22 * 32 + lane] = (int)gtri;
+    }
+    int end = n;   // running end of the samples up to this lane's triangle
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int o = __shfl_up_sync(0xffffffffu, end, d);
+        if (lane >= d) end += o;
+    }
+    const int total = __shfl_sync(0xffffffffu, end, 31), first = end - n;
+    __syncwarp();
+    uint32_t frags = 0;
+    for (int base = 0; base < total; base += 32) {
+        const int k = base + lane;
+        // the triangle of sample k: the number of lanes whose samples end at or before k
+        int src = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(0xffffffffu, end, src + step - 1) <= k) src += step;
+        const int i = k - __shfl_sync(0xffffffffu, first, src);
+        if (k >= total) continue;
+        const int cols = si[18 * 32 + src];
+        // i / cols from a reciprocal: i + 0.5 is at least 0.5 from a multiple of cols, far
+        // beyond the rounding error for the sizes a direct triangle has
+        const int row = (int)(((float)i + 0.5f) * __frcp_rn((float)cols));
+        const int x = si[16 * 32 + src] + (i - row * cols), y = si[17 * 32 + src] + row;
+        TriRecord t;
+        t.v1x = sf[0 * 32 + src]; t.v1y = sf[1 * 32 + src]; t.v2x = sf[2 * 32 + src]; t.v2y = sf[3 * 32 + src];
+        t.v3x = sf[4 * 32 + src]; t.v3y = sf[5 * 32 + src];
+        t.dx0 = sf[6 * 32 + src]; t.dy0 = sf[7 * 32 + src]; t.dx1 = sf[8 * 32 + src]; t.dy1 = sf[9 * 32 + src];
+        t.dx2 = sf[10 * 32 + src]; t.dy2 = sf[11 * 32 + src];
+        t.v1z = sf[12 * 32 + src]; t.dz2 = sf[13 * 32 + src]; t.dz3 = sf[14 * 32 + src]; t.a = sf[15 * 32 + src];
+        const uint32_t id = (uint32_t)si[22 * 32 + src];
+        unsigned long long *rowu = keys + (size_t)y * pitch, *rown = rowu + pitch;
+        auto fold = [&](int xx, const EdgeVals &e) {
+            if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
+                ++frags;
+                const float z = interp_z(t.v1z, t.dz2, t.dz3, t.a, e.w1, e.w2);
+                if (z < kFltMax) {
+                    const uint32_t nw = 2 * xx < w ? 1u : 0u;
+                    red_min_u64((nw ? rowu : rown) + key_col(nw ? 2 * xx : 2 * xx - w, tw),
+                                (unsigned long long)make_key(z, id, nw));
+                }
+            }
+        };
+        const EdgeVals e = eval_edges(t, (float)x, (float)y);
+        fold(x, e);
+        if (x == si[19 * 32 + src]) {
+            const uint32_t mask = (uint32_t)si[21 * 32 + src];
+            const uint32_t neg = (e.w0 < 0.0f ? 1u : 0u) | (e.w1 < 0.0f ? 2u : 0u) | (e.w2 < 0.0f ? 4u : 0u);
+            if (!(neg & mask)) {
+                // the row goes on past the probe column (rare: edge values that round to
+                // >= 0 right of max.x): walk it as direct_raster does
+                const EdgeRows c = edge_rows(t, (float)y);
+                const int xe2 = si[20 * 32 + src];
+                for (int xx = x + 1; xx < xe2; ++xx) {
+                    const EdgeVals e2 = eval_edges_row(t, c, (float)xx);
+                    const uint32_t n2 = (e2.w0 < 0.0f ? 1u : 0u) | (e2.w1 < 0.0f ? 2u : 0u) | (e2.w2 < 0.0f ? 4u : 0u);
+                    if (n2 & mask) break;
+                    fold(xx, e2);
+                }
+            }
+        }
+    }
+    __syncwarp();   // the stage is reused by the warp's next call
     return frags;
 }
 

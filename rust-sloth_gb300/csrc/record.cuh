@@ -140,8 +140,7 @@ __device__ __forceinline__ uint32_t load_rgb(const uint8_t *rgb, uint32_t t)
 // (setup_smem_bytes): per slot the triangle index, its packed colour and its three
 // transformed vertices, as 11 arrays of cap words so that consecutive slots fall in
 // different banks.  Phase 2 reads a queued triangle from here, not from global memory.
-// Indexing the shared array itself keeps the accesses 32-bit shared ones.
-extern __shared__ uint32_t setup_smem[];
+// setup_smem (direct.cuh) is indexed itself, which keeps the accesses 32-bit shared ones.
 
 struct SetupStash {
     uint32_t cap;

@@ -87,7 +87,7 @@ __device__ __forceinline__ void triangle_vertices(const MeshDev &mesh, const flo
 template <bool kDirect>
 __device__ __forceinline__ void setup_triangle(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
                                                const BinBuffers &bb, bool live, uint32_t t, float4 p1, float4 p2,
-                                               float4 p3, uint32_t rgb)
+                                               float4 p3, uint32_t rgb, uint32_t stage)
 {
     bool large = false, direct = false;
     TriRecord r;
@@ -110,10 +110,9 @@ __device__ __forceinline__ void setup_triangle(uint32_t tri_base, const FrameGeo
     }
     // the smallest triangles fold their samples into the global keys here (direct.cuh)
     if (kDirect && __any_sync(0xffffffffu, direct)) {
-        const uint32_t frags = direct ? direct_raster(r, tri_base + t, g.w, g.pitch, g.tw,
-                                                      reinterpret_cast<unsigned long long *>(fb.keys), dw.xend,
-                                                      dw.exit_mask)
-                                      : 0u;
+        const uint32_t frags = direct_raster_warp(direct, r, tri_base + t, g.w, g.pitch, g.tw,
+                                                  reinterpret_cast<unsigned long long *>(fb.keys), dw.xend,
+                                                  dw.exit_mask, stage);
         add_frags_warp(frags, fb.fragments);
     }
 }
@@ -173,7 +172,8 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
             float4 p1, p2, p3;
             uint32_t rgb = 0, t = 0;
             if (q < nq) t = st.get(q, p1, p2, p3, rgb);
-            setup_triangle<kDirect>(tri_base, g, fb, bb, q < nq, t, p1, p2, p3, rgb);
+            setup_triangle<kDirect>(tri_base, g, fb, bb, q < nq, t, p1, p2, p3, rgb,
+                                    11u * cap + (threadIdx.x >> 5) * (uint32_t)kDirectStageWords);
         }
         if (!kChunks) break;
         base = total;
@@ -284,6 +284,22 @@ cudaError_t launch_vertex_transform(const MeshDev &mesh, const Mat4 &M, float4 *
     return cudaGetLastError();
 }
 
+cudaError_t prepare_setup_kernels()
+{
+    static std::atomic<uint32_t> done{0};   // devices prepared (bit per device < 32)
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint32_t bit = dev < 32 ? 1u << dev : 0u;
+    if (bit && (done.load() & bit)) return cudaSuccess;
+    const int bytes = (int)setup_smem_bytes(kMaxTrianglesPerBlock, true);
+    if ((e = cudaFuncSetAttribute(setup_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) ||
+        (e = cudaFuncSetAttribute(setup_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    done.fetch_or(bit);
+    return cudaSuccess;
+}
+
 cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, uint32_t tri_base,
                          const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
                          cudaStream_t s, int tpb)
@@ -291,7 +307,7 @@ cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, u
     if (mesh.ntri == 0) return cudaSuccess;
     if (!valid_triangles_per_block(tpb)) return cudaErrorInvalidValue;
     const uint32_t blocks = (mesh.ntri + tpb - 1) / tpb;
-    const size_t smem = setup_smem_bytes(tpb);   // at most 45,056 bytes: no opt-in needed
+    const size_t smem = setup_smem_bytes(tpb, g.direct_max > 0);   // prepare_setup_kernels: above 48 KB
     const dim3 grid(blocks), block(setup_block_threads(tpb));
     const bool chunks = tpb > kSetupChunk;
     if (g.direct_max > 0) {

@@ -466,6 +466,7 @@ sloth_status sloth_ctx_create(sloth_ctx **out, int device, void *stream)
     if (cudaMallocHost(&ctx->h_total, sizeof(uint32_t)) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->total_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->scan_ev, cudaEventDisableTiming) != cudaSuccess ||
+        prepare_setup_kernels() != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->nl_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||

@@ -127,7 +127,15 @@ __host__ __device__ inline int setup_block_threads(int tpb) { return tpb < kSetu
 // their transformed vertices and colour (record.cuh: SetupStash, 44 bytes a triangle).
 constexpr int kSetupChunk = 1024;
 __host__ __device__ inline int setup_chunk(int tpb) { return tpb < kSetupChunk ? tpb : kSetupChunk; }
-__host__ __device__ inline size_t setup_smem_bytes(int tpb) { return 44u * (size_t)setup_chunk(tpb); }
+// Dynamic shared memory of a setup block: the stash, and with the direct path one stage of
+// 23 x 32 words per warp (direct.cuh) after it.
+__host__ __device__ inline size_t setup_smem_bytes(int tpb, bool direct = false)
+{
+    return 44u * (size_t)setup_chunk(tpb) + (direct ? (size_t)(setup_block_threads(tpb) / 32) * 23u * 32u * 4u : 0u);
+}
+// Sets the shared-memory limit of the setup kernels with the direct path (above the 48 KB
+// default), once per device; call before the first launch and outside stream capture.
+cudaError_t prepare_setup_kernels();
 
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked
 // up once per device): grids of the grid-stride kernels are sized by it.
