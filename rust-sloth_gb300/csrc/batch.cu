@@ -49,8 +49,10 @@ __global__ void __launch_bounds__(256) batch_vertex_kernel(BatchDev b, const int
                                      row_dot(&M.m[8], xs[k], ys[k], zs[k]), 0.0f);
 }
 
-// The three transformed vertices of triangle t of draw d (the vertex kernel's output).
-__device__ __forceinline__ void batch_triangle_vertices(const BatchDev &b, const BatchDraw &d, uint32_t t, float4 &p1,
+// The three vertices of triangle t of draw d transformed by the draw's matrix M in place
+// (the vertex kernel's operations): a mesh shared by many views stays in L2, and no
+// transformed-vertex buffer is written and read back for the render.
+__device__ __forceinline__ void batch_triangle_vertices(const BatchDraw &d, const Mat4 &M, uint32_t t, float4 &p1,
                                                         float4 &p2, float4 &p3)
 {
     uint32_t i1, i2, i3;
@@ -61,10 +63,9 @@ __device__ __forceinline__ void batch_triangle_vertices(const BatchDev &b, const
     } else {
         i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
     }
-    const float4 *tv = b.tv + d.vert_off;
-    p1 = __ldg(tv + i1);
-    p2 = __ldg(tv + i2);
-    p3 = __ldg(tv + i3);
+    p1 = transform_vertex(d.mesh, M, i1);
+    p2 = transform_vertex(d.mesh, M, i2);
+    p3 = transform_vertex(d.mesh, M, i3);
 }
 
 // One triangle t of draw d with transformed vertices p1, p2, p3 and packed colour rgb
@@ -125,7 +126,9 @@ __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFi
     // reloaded from global memory after each of the block's record stores
     __shared__ BatchDraw sd;
     __shared__ BatchFrame sf;
+    __shared__ Mat4 sm;
     const int2 blk = blocks[blockIdx.x];
+    if (threadIdx.x < 16) sm.m[threadIdx.x] = b.mats[blk.x].m[threadIdx.x];
     const uint32_t cap = (uint32_t)setup_chunk(b.tpb);
     const SetupStash st{cap};
     if (threadIdx.x == 0) {
@@ -147,20 +150,20 @@ __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFi
             float4 a1, a2, a3, b1, b2, b3;
             uint32_t ca = 0, cb = 0;
             if (lt) {
-                batch_triangle_vertices(b, d, t, a1, a2, a3);
+                batch_triangle_vertices(d, sm, t, a1, a2, a3);
                 ca = load_rgb(d.mesh.rgb, t);
             }
             if (lu) {
-                batch_triangle_vertices(b, d, u, b1, b2, b3);
+                batch_triangle_vertices(d, sm, u, b1, b2, b3);
                 cb = load_rgb(d.mesh.rgb, u);
             }
             int4 row4;
             const bool kt = lt && needs_setup(a1, a2, a3, f.g.w, f.g.h, row4);
-            if (lt && !kt) reinterpret_cast<int4 *>(f.fb.records + d.local_base + t)[4] = row4;
+            if (lt && !kt) store_row4(f.fb.records + d.local_base + t, row4);
             if (lt) f.fb.rows[d.local_base + t] = pack_rows(row4.z, row4.w);
             stash_push(st, &sq_n, base, kt, t, a1, a2, a3, ca);
             const bool ku = lu && needs_setup(b1, b2, b3, f.g.w, f.g.h, row4);
-            if (lu && !ku) reinterpret_cast<int4 *>(f.fb.records + d.local_base + u)[4] = row4;
+            if (lu && !ku) store_row4(f.fb.records + d.local_base + u, row4);
             if (lu) f.fb.rows[d.local_base + u] = pack_rows(row4.z, row4.w);
             stash_push(st, &sq_n, base, ku, u, b1, b2, b3, cb);
         }

@@ -42,6 +42,12 @@ struct sloth_batch {
     std::vector<uint64_t> cell_off, z_off;    // per frame
     uint32_t total_tiles = 0;
     uint64_t total_cells = 0, total_z = 0, total_keys = 0, total_nl = 0, total_rec = 0, total_vert = 0;
+    // runs of consecutive frames' keys with the same width parity: (first key, keys, even width)
+    struct KeyRun {
+        uint64_t off, n;
+        bool even;
+    };
+    std::vector<KeyRun> key_runs;
     int max_nl = 1;
 
     // device memory
@@ -49,7 +55,7 @@ struct sloth_batch {
     BatchDraw *d_draws = nullptr;
     Mat4 *d_mats = nullptr;
     Mat4 *h_mats = nullptr;                   // pinned
-    float4 *tv = nullptr;
+    float4 *tv = nullptr;                     // transformed vertices: written for shading only (want_tv)
     TriRecord *records = nullptr;
     uint32_t *rows = nullptr;                 // packed sample rows per record (setup -> newline)
     uint64_t *keys = nullptr;
@@ -86,6 +92,7 @@ struct sloth_batch {
     uint32_t ndiff_blk = 0;
     uint2 *vis = nullptr;                     // stored visibility, one per depth cell
     bool vis_valid = false;                   // vis holds the last render's visibility
+    bool want_tv = false;                     // shading has been used: renders fill tv
 
     FlushScratch flush;
 };
@@ -190,6 +197,7 @@ sloth_status build(sloth_batch *b, int shape)
     const int tw = kTileShapes[shape][0], th = kTileShapes[shape][1];
     const uint32_t nf = (uint32_t)b->frames.size(), nd = (uint32_t)b->meshes.size();
     b->hframes.assign(nf, BatchFrame{});
+    b->key_runs.clear();
     b->cell_off.assign(nf + 1, 0);
     b->z_off.assign(nf + 1, 0);
     std::vector<uint64_t> key_off(nf), nl_off(nf), rec_off(nf);
@@ -223,6 +231,12 @@ sloth_status build(sloth_batch *b, int shape)
         bf.z_off = zs;
         tile_off[f] = tiles;
         key_off[f] = keys;
+        {
+            const uint64_t nk = (uint64_t)g.pitch * g.nty * th;
+            const bool even = !(g.w & 1);
+            if (!b->key_runs.empty() && b->key_runs.back().even == even) b->key_runs.back().n += nk;
+            else b->key_runs.push_back({keys, nk, even});
+        }
         nl_off[f] = nl;
         rec_off[f] = rec;
         b->cell_off[f] = cells;
@@ -344,7 +358,8 @@ BatchDev dev_view(sloth_batch *b)
     return d;
 }
 
-// Stage 1: reset, matrices, vertices, setup, newline, large counts, scan.
+// Stage 1: reset, matrices, vertices (once shading wants them), setup, newline, large
+// counts, scan.
 cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
 {
     cudaError_t e;
@@ -352,7 +367,8 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     if (b->direct_max > 0) {
         // small triangles fold into the global keys during setup: every tile's keys start
         // empty and current (kBatchGen is 0x01 in every byte)
-        if ((e = cudaMemsetAsync(b->keys, 0xff, (size_t)b->total_keys * 8, s))) return e;
+        for (const auto &kr : b->key_runs)
+            if ((e = launch_clear_keys(b->keys + kr.off, kr.n, kTileShapes[b->shape][0], kr.even, s))) return e;
         if ((e = cudaMemsetAsync(b->tile_gen, 0x01, (size_t)b->total_tiles * 4, s))) return e;
     } else {
         if ((e = cudaMemsetAsync(b->tile_gen, 0, (size_t)b->total_tiles * 4, s))) return e;
@@ -364,7 +380,7 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
     if ((e = cudaMemsetAsync(b->overflow, 0, 4, s))) return e;
     if ((e = cudaMemcpyAsync(b->d_mats, b->h_mats, b->meshes.size() * sizeof(Mat4), cudaMemcpyHostToDevice, s)))
         return e;
-    if ((e = launch_batch_vertex(d, b->blk[0], b->nblk[0], s))) return e;
+    if (b->want_tv && (e = launch_batch_vertex(d, b->blk[0], b->nblk[0], s))) return e;
     if ((e = launch_batch_setup(d, b->blk[1], b->nblk[1], s))) return e;
     if ((e = cudaEventRecord(b->ev_setup, s))) return e;
     if ((e = cudaStreamWaitEvent(b->nl_s, b->ev_setup, 0))) return e;
@@ -475,7 +491,19 @@ sloth_status diff_prepare(sloth_batch *b, const float *vertex_rgb, const float *
         b->ndiff_blk = (uint32_t)t.size();
     }
     // the keys of the last render must be complete (re-render if its entries overflowed)
-    return settle(b);
+    sloth_status st = settle(b);
+    if (st != SLOTH_OK) return st;
+    if (!b->want_tv) {
+        // the first shading of this batch: transform the vertices the last render drew, and
+        // let every later render do it too (the graph is captured again)
+        BCU(b, launch_batch_vertex(dev_view(b), b->blk[0], b->nblk[0], b->stream));
+        b->want_tv = true;
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+    }
+    return SLOTH_OK;
 }
 
 

@@ -9,6 +9,7 @@
 #include "bounds.cuh"
 #include "direct.cuh"
 #include "sloth_internal.cuh"
+#include "sloth_kernels.h"
 
 namespace sloth {
 
@@ -72,7 +73,8 @@ __device__ __forceinline__ int sat_hi(float f)
 
 // Stores a record.  A triangle with no tile (culled, empty sample range) only ever has its
 // sample range read -- by the newline and fill kernels, which stop there -- so only that
-// row is written.  A direct triangle (direct.cuh) is never binned nor rasterized again:
+// row is written, with zeros in row 5 beside it (store_row4: a whole 32-byte sector, which
+// the memory writes back without reading it first).  A direct triangle (direct.cuh) is never binned nor rasterized again:
 // only the rows the resolve (0-1, 5) and the newline and fill kernels (4) read are written.
 __device__ __forceinline__ void store_record(TriRecord *dst, const TriRecord &r, uint32_t ntiles, bool direct = false)
 {
@@ -87,7 +89,17 @@ __device__ __forceinline__ void store_record(TriRecord *dst, const TriRecord &r,
         *dst = r;
     } else {
         d[4] = make_int4(r.x0, r.xe, r.y0, r.y1);
+        d[5] = make_int4(0, 0, 0, 0);
     }
+}
+
+// Record rows 4 (the sample range, row4) and 5 (zeros) of a triangle with nothing to
+// rasterize (store_record).
+__device__ __forceinline__ void store_row4(TriRecord *dst, int4 row4)
+{
+    int4 *d = reinterpret_cast<int4 *>(dst);
+    d[4] = row4;
+    d[5] = make_int4(0, 0, 0, 0);
 }
 
 // The first steps of build_record, for a setup kernel that sets triangles aside before the
@@ -284,6 +296,13 @@ __device__ __forceinline__ float row_dot(const float *m, float x, float y, float
     acc = fadd(fmul(m[2], z), acc);
     acc = fadd(fmul(m[3], 1.0f), acc);
     return acc;
+}
+
+// One vertex transformed in place: (M*v).xyz with the vertex kernels' operations.
+__device__ __forceinline__ float4 transform_vertex(const MeshDev &mesh, const Mat4 &M, uint32_t i)
+{
+    const float x = __ldg(mesh.x + i), y = __ldg(mesh.y + i), z = __ldg(mesh.z + i);
+    return make_float4(row_dot(&M.m[0], x, y, z), row_dot(&M.m[4], x, y, z), row_dot(&M.m[8], x, y, z), 0.0f);
 }
 
 // Count the small triangle's tiles (bin count pass).

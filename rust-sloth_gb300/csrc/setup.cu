@@ -53,13 +53,6 @@ __device__ __forceinline__ Viewport to_vp(const FrameGeom &g)
     return Viewport{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
 }
 
-// One vertex of a soup transformed in place: (M*v).xyz with the vertex kernel's operations.
-__device__ __forceinline__ float4 transform_vertex(const MeshDev &mesh, const Mat4 &M, uint32_t i)
-{
-    const float x = __ldg(mesh.x + i), y = __ldg(mesh.y + i), z = __ldg(mesh.z + i);
-    return make_float4(row_dot(&M.m[0], x, y, z), row_dot(&M.m[4], x, y, z), row_dot(&M.m[8], x, y, z), 0.0f);
-}
-
 // The three transformed vertices of triangle t.  tv null (soups): the thread transforms
 // them itself, which saves the vertex kernel and its round trip through memory.
 __device__ __forceinline__ void triangle_vertices(const MeshDev &mesh, const float4 *__restrict__ tv, const Mat4 &M,
@@ -157,11 +150,11 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
             }
             int4 row4;
             const bool kt = lt && needs_setup(a1, a2, a3, g.w, g.h, row4);
-            if (lt && !kt) reinterpret_cast<int4 *>(fb.records + tri_base + t)[4] = row4;
+            if (lt && !kt) store_row4(fb.records + tri_base + t, row4);
             if (lt) fb.rows[tri_base + t] = pack_rows(row4.z, row4.w);
             stash_push(st, &sq_n, base, kt, t, a1, a2, a3, ca);
             const bool ku = lu && needs_setup(b1, b2, b3, g.w, g.h, row4);
-            if (lu && !ku) reinterpret_cast<int4 *>(fb.records + tri_base + u)[4] = row4;
+            if (lu && !ku) store_row4(fb.records + tri_base + u, row4);
             if (lu) fb.rows[tri_base + u] = pack_rows(row4.z, row4.w);
             stash_push(st, &sq_n, base, ku, u, b1, b2, b3, cb);
         }
@@ -258,6 +251,31 @@ cudaError_t launch_frame_reset(const FrameBuffers &fb, const BinBuffers &bb, uin
     const uint32_t n = max(frame ? nl_nodes : 1u, (draw || tiles_current) ? ntiles : 1u);
     frame_reset_kernel<<<(n + 255) / 256, 256, 0, s>>>(fb, bb, nl_nodes, ntiles, frame ? 1 : 0, draw ? 1 : 0,
                                                        tiles_current ? 1 : 0);
+    return cudaGetLastError();
+}
+
+// Keys the samples can write set to the empty key (all bytes 0xff) in a run of tile rows of
+// tw cells: the first half of every run of tw keys (key_col: the even columns, all that a
+// frame of even width writes).  Two keys per store; n4 = the 16-byte stores, tw >= 8.
+__global__ void __launch_bounds__(256) clear_live_keys_kernel(uint4 *keys, uint64_t n4, uint32_t half_shift)
+{
+    const uint4 empty = make_uint4(~0u, ~0u, ~0u, ~0u);
+    const uint64_t mask = (1ull << half_shift) - 1ull;   // stores per half run
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n4; v += (uint64_t)gridDim.x * blockDim.x)
+        keys[((v >> half_shift) << (half_shift + 1)) | (v & mask)] = empty;
+}
+
+cudaError_t launch_clear_keys(uint64_t *keys, uint64_t ncells, int tw, bool even_width, cudaStream_t s)
+{
+    if (ncells == 0) return cudaSuccess;
+    if (!even_width) return cudaMemsetAsync(keys, 0xff, ncells * sizeof(uint64_t), s);
+    uint32_t half_shift = 0;   // log2(tw / 4): 16-byte stores in half a run of tw keys
+    while ((4u << half_shift) < (uint32_t)tw) ++half_shift;
+    const uint64_t n4 = ncells / 4;   // two keys per store, half of the keys
+    uint64_t blocks = (n4 + 255) / 256;
+    const uint64_t cap = 16ull * (uint64_t)device_sm_count();
+    if (blocks > cap) blocks = cap;
+    clear_live_keys_kernel<<<(unsigned)blocks, 256, 0, s>>>(reinterpret_cast<uint4 *>(keys), n4, half_shift);
     return cudaGetLastError();
 }
 

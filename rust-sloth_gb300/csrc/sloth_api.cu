@@ -285,8 +285,8 @@ static sloth_status apply_resets(sloth_ctx *ctx, bool draw)
     // keys valid for this generation: cleared once per frame, the tiles made current
     const bool tiles = draw && ctx->g.direct_max > 0 && !ctx->keys_current;
     if (tiles)
-        CU(ctx, cudaMemsetAsync(ctx->fb.keys, 0xff,
-                                (size_t)ctx->g.pitch * ctx->g.nty * ctx->g.th * sizeof(uint64_t), ctx->stream));
+        CU(ctx, launch_clear_keys(ctx->fb.keys, (uint64_t)ctx->g.pitch * ctx->g.nty * ctx->g.th, ctx->g.tw,
+                                  !(ctx->g.w & 1), ctx->stream));
     CU(ctx, timed(ctx, "reset", [&] {
            return launch_frame_reset(ctx->fb, ctx->bb, 2u * (uint32_t)ctx->g.nl_size,
                                      (uint32_t)(ctx->g.ntx * ctx->g.nty), frame, draw, tiles, ctx->stream);

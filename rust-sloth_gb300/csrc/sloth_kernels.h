@@ -144,6 +144,10 @@ int device_sm_count();
 // frame resets (error word, fragments, newline tree) and draw resets (tile counts, large
 // queue counters), either or both, in one launch; tiles_current also sets every tile's
 // generation to the current one (its keys were cleared to the empty key before).
+// Every key a sample can write in ncells cells of tile rows of tw cells (a multiple of tw)
+// set to the empty key: the even half of each tile row when the frame's width is even
+// (key_col), all of them otherwise.
+cudaError_t launch_clear_keys(uint64_t *keys, uint64_t ncells, int tw, bool even_width, cudaStream_t s);
 cudaError_t launch_frame_reset(const FrameBuffers &fb, const BinBuffers &bb, uint32_t nl_nodes, uint32_t ntiles,
                                bool frame, bool draw, bool tiles_current, cudaStream_t s);
 
