@@ -357,9 +357,10 @@ __global__ void __launch_bounds__(256) batch_resolve_kernel(BatchDev b, const in
     const uint64_t ncells = f.g.image ? nz + f.g.h : nz;
     const uint64_t end = min(ncells, (uint64_t)blk.y + kBatchResolveChunk);   // chunks start on runs
     if (!(f.g.w & 1)) {
-        // an even-width frame by pairs of cells (resolve_even), four per thread
-        static_assert(kBatchResolveChunk == 2 * 4 * 256, "four pairs per thread and block");
-        resolve_even<4>(f.g, f.fb, (uint64_t)blk.y / 2 + threadIdx.x, blockDim.x, (end + 1) / 2, f.vec != 0);
+        // an even-width frame by pairs of cells (resolve_even), four per thread at a time
+        const uint64_t pend = (end + 1) / 2;
+        for (uint64_t p0 = (uint64_t)blk.y / 2; p0 < pend; p0 += 4 * blockDim.x)
+            resolve_even<4>(f.g, f.fb, p0 + threadIdx.x, blockDim.x, pend, f.vec != 0);
         return;
     }
     const int lane = threadIdx.x & 31;

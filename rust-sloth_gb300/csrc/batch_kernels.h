@@ -67,6 +67,6 @@ cudaError_t launch_batch_resolve(const BatchDev &b, const int2 *blocks, uint32_t
 cudaError_t prepare_batch_kernels();
 
 constexpr uint32_t kBatchNewlineChunk = 8192;   // triangles per newline block
-constexpr uint32_t kBatchResolveChunk = 2048;   // cells per resolve block
+constexpr uint32_t kBatchResolveChunk = 8192;   // cells per resolve block (four rounds of its threads)
 
 }  // namespace sloth
