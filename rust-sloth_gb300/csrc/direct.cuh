@@ -3,9 +3,9 @@
 // Most triangles of a finely tessellated mesh cover a handful of samples.  Binning them
 // (a tile count, a scan, an entry per tile, a sort in the tile's CTA) costs far more than
 // their samples do.  A triangle whose sample range [x0,xe) x [y0,y1) holds at most
-// FrameGeom::direct_max samples is therefore rasterized by the thread that set it up: it
-// runs the reference's loop body (src/rasterizer.rs:69-86) over its range and folds each
-// covered sample's depth key into the global key of its target cell with a 64-bit
+// FrameGeom::direct_max samples is therefore rasterized by the warp that set it up: the
+// warp runs the reference's loop body (src/rasterizer.rs:69-86) over the range and folds
+// each covered sample's depth key into the global key of its target cell with a 64-bit
 // atomicMin.  The minimum of a cell's keys does not depend on the order of the folds, so
 // the result is the same as folding the triangle in its tile's CTA; the tile raster later
 // loads those keys and folds the binned triangles on top.
@@ -26,50 +26,22 @@ __host__ __device__ __forceinline__ bool is_direct(int x0, int xe, int y0, int y
     return x0 < xe && y0 < y1 && (uint32_t)(xe - x0) * (uint32_t)(y1 - y0) <= (uint32_t)direct_max;
 }
 
-// The samples of rows [y0,y1) from column x0 to xend (exclusive) in the reference's
-// row-major order (the order does not matter for the result); a row ends early at the
-// first column where an edge of exit_mask (bit i: edge i) is negative -- edges whose value
-// only falls along the row, so no later sample of the row can be covered.  Sample (x, y)
-// writes depth cell y*w + 2x (src/rasterizer.rs:80): row y, column 2x when 2x < w, else
-// row y+1, column 2x-w, stored at key_col of its column for tile width tw.  Returns the
-// covered samples.
-__device__ __forceinline__ uint32_t direct_raster(const TriRecord &r, uint32_t gtri, int w, int pitch, int tw,
-                                                 unsigned long long *keys, int xend, uint32_t exit_mask)
-{
-    uint32_t frags = 0;
-    for (int y = r.y0; y < r.y1; ++y) {
-        const EdgeRows c = edge_rows(r, (float)y);
-        unsigned long long *rowu = keys + (size_t)y * pitch, *rown = rowu + pitch;
-        for (int x = r.x0; x < xend; ++x) {
-            const EdgeVals e = eval_edges_row(r, c, (float)x);
-            const uint32_t neg = (e.w0 < 0.0f ? 1u : 0u) | (e.w1 < 0.0f ? 2u : 0u) | (e.w2 < 0.0f ? 4u : 0u);
-            if (neg & exit_mask) break;
-            if (e.w0 >= 0.0f && e.w1 >= 0.0f && e.w2 >= 0.0f) {
-                ++frags;
-                const float z = interp_z(r.v1z, r.dz2, r.dz3, r.a, e.w1, e.w2);
-                if (z < kFltMax) {
-                    // unwrapped: row y, column 2x; wrapped: row y+1, column 2x-w
-                    const uint32_t nw = 2 * x < w ? 1u : 0u;
-                    red_min_u64((nw ? rowu : rown) + key_col(nw ? 2 * x : 2 * x - w, tw),
-                                (unsigned long long)make_key(z, gtri, nw));
-                }
-            }
-        }
-    }
-    return frags;
-}
-
 // The direct triangles of a warp folded together (called by all 32 lanes; lanes with
-// mine false bring none).  Each triangle's samples are its rows [y0, y1) times the columns
-// [x0, xs): xs = xend for a triangle walked over its stored range (exit_mask 0); with row
-// exits, xs = min(r.xe + 1, xend), the unproven end plus one probe column.  The warp walks
+// mine false bring none).  A triangle's samples lie in rows [y0, y1) from column x0 up to
+// xend (exclusive); with exit_mask set a row ends at the first column where an edge of the
+// mask (bit i: edge i, edges whose value only falls along a row) is negative.  Sample
+// (x, y) writes depth cell y*w + 2x (src/rasterizer.rs:80): row y, column 2x when 2x < w,
+// else row y+1, column 2x-w, stored at key_col of its column for tile width tw.  Each
+// triangle's walked samples are its rows times the columns [x0, xs): xs = xend for a
+// triangle walked over its stored range (exit_mask 0); with row exits, xs =
+// min(r.xe + 1, xend), the unproven end plus one probe column.  The warp walks
 // the concatenation of all its triangles' samples 32 at a time, each lane finding its
 // triangle by a binary search over the running ends, so that the lanes stay busy and one
 // reduction instruction covers neighbouring samples of a few triangles (fewer memory
 // requests).  A covered sample is never past a row's exit (an exit edge, once negative,
 // stays negative along the row), so walking every column up to the probe folds the same
-// samples as the row walk of direct_raster.  When the probe column still has no exit edge
-// negative, the lane that tested it walks the rest of that row as direct_raster does.
+// samples as a row walk with exits.  When the probe column still has no exit edge
+// negative, the lane that tested it walks the rest of that row, up to its first exit.
 // The warp stages its triangles in kDirectStageWords words of the setup kernels' dynamic
 // shared memory from word `stage` on (structure of arrays: field f of lane l at f*32 + l,
 // so lanes reading one triangle share a broadcast and different triangles fall in
@@ -155,7 +127,7 @@ __device__ __forceinline__ uint32_t direct_raster_warp(bool mine, const TriRecor
             const uint32_t neg = (e.w0 < 0.0f ? 1u : 0u) | (e.w1 < 0.0f ? 2u : 0u) | (e.w2 < 0.0f ? 4u : 0u);
             if (!(neg & mask)) {
                 // the row goes on past the probe column (rare: edge values that round to
-                // >= 0 right of max.x): walk it as direct_raster does
+                // >= 0 right of max.x): walk it up to its first exit
                 const EdgeRows c = edge_rows(t, (float)y);
                 const int xe2 = si[20 * 32 + src];
                 for (int xx = x + 1; xx < xe2; ++xx) {
