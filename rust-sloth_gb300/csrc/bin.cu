@@ -205,35 +205,25 @@ bin_items_kernel(uint32_t n, FrameGeom g, FrameBuffers fb, BinBuffers bb)
     }
 }
 
-// Triangles of the draw, tpb per block (setup_kernel's partition): small triangles write
-// their tile entries.
-__device__ __forceinline__ void fill_triangle(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
-                                              const FrameBuffers &fb, const BinBuffers &bb, uint32_t t)
-{
-    const uint32_t gtri = tri_base + t;
-    const Viewport vp = vp_of(g);
-    const bool live = t < ntri;
-    TriRecord r;
-    TileSpan sp{};
-    if (live) {
-        // the whole record in one round trip (a triangle without tiles has only its
-        // sample range stored, and nothing else of it is used)
-        const float4 *p = reinterpret_cast<const float4 *>(fb.records + gtri);
-        float4 *o = reinterpret_cast<float4 *>(&r);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) o[k] = __ldg(p + k);
-        sp = tile_span(vp, r);
-        if (is_direct(r.x0, r.xe, r.y0, r.y1, g.direct_max)) sp.ntiles = 0;   // rasterized by setup
-    }
-    fill_small_warp(live && !sp.large && sp.ntiles != 0, r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
-}
-
+// The small binned triangles setup listed, 256 per block and round (grid-stride): their
+// tile entries.  Only their records are read.
 __global__ void __launch_bounds__(kSetupThreads, kFillMinBlocks)
-bin_fill_kernel(uint32_t ntri, uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb, int tpb)
+bin_fill_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
 {
-    for (uint32_t t = blockIdx.x * (uint32_t)tpb + threadIdx.x; t < (blockIdx.x + 1u) * (uint32_t)tpb;
-         t += blockDim.x)
-        fill_triangle(ntri, tri_base, g, fb, bb, t);
+    const uint32_t n = bb.large_count[2];
+    const Viewport vp = vp_of(g);
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool live = i < n;
+        const uint32_t gtri = tri_base + (live ? bb.fill_list[i] : 0u);
+        TriRecord r;
+        TileSpan sp{};
+        if (live) {
+            r = load_record(fb.records, gtri);
+            sp = tile_span(vp, r);
+        }
+        fill_small_warp(live, r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
+    }
 }
 
 static int large_grid()
@@ -262,12 +252,10 @@ cudaError_t launch_bin_items(uint32_t ntiles, const FrameGeom &g, const FrameBuf
     return cudaGetLastError();
 }
 
-cudaError_t launch_bin_fill(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
-                            const FrameBuffers &fb, const BinBuffers &bb, cudaStream_t s, int tpb)
+cudaError_t launch_bin_fill(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
+                            cudaStream_t s)
 {
-    if (ntri == 0) return cudaSuccess;
-    if (!valid_triangles_per_block(tpb)) return cudaErrorInvalidValue;
-    bin_fill_kernel<<<(ntri + tpb - 1) / tpb, setup_block_threads(tpb), 0, s>>>(ntri, tri_base, g, fb, bb, tpb);
+    bin_fill_kernel<<<kFillMinBlocks * 2 * device_sm_count(), kSetupThreads, 0, s>>>(tri_base, g, fb, bb);
     return cudaGetLastError();
 }
 

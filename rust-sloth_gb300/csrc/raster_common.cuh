@@ -109,16 +109,6 @@ __device__ __forceinline__ void fence_proxy_async_smem()
 constexpr uint32_t kWaitPolls = 1u << 22;   // polls of a bulk-copy barrier before giving up
 constexpr uint32_t kTestWaitPolls = 1u << 10;   // the same under the wait test hook
 
-__device__ __forceinline__ TriRecord load_record(const TriRecord *__restrict__ recs, uint32_t i)
-{
-    const float4 *p = reinterpret_cast<const float4 *>(recs + i);
-    TriRecord r;
-    float4 *o = reinterpret_cast<float4 *>(&r);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) o[k] = __ldg(p + k);
-    return r;
-}
-
 // One sample of the reference's loop body: edge test, depth, key folded into the tile.
 // With a depth bound zb of the triangle in this tile (0: none), a cell already nearer
 // than zb is passed over before the edge test: no depth of the triangle can beat it.

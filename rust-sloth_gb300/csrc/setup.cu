@@ -94,8 +94,20 @@ __device__ __forceinline__ void setup_triangle(uint32_t tri_base, const FrameGeo
         store_record(fb.records + tri_base + t, r, sp.ntiles, direct);
         large = sp.large;
     }
-    // binning: count tiles of small triangles here, queue the rest for warps
-    count_small_tiles_warp(live && !large && !direct, r, vp, sp, bb.tile_count);
+    // binning: count tiles of small triangles here and list them for the fill, queue the
+    // rest for warps
+    const bool binned = live && !large && !direct && sp.ntiles != 0;
+    count_small_tiles_warp(binned, r, vp, sp, bb.tile_count);
+    if (bb.fill_list) {
+        const unsigned bm = __ballot_sync(0xffffffffu, binned);
+        if (bm) {
+            const int lane = threadIdx.x & 31;
+            uint32_t first = 0;
+            if (lane == 0) first = atomicAdd(&bb.large_count[2], (uint32_t)__popc(bm));
+            first = __shfl_sync(0xffffffffu, first, 0);
+            if (binned) bb.fill_list[first + __popc(bm & ((1u << lane) - 1u))] = t;
+        }
+    }
     // warp-ballot compaction of the large-triangle queue
     if (__any_sync(0xffffffffu, large)) {
         const int q = large_slot(large, sp.ntiles, bb.large_count, bb.large_cap);
@@ -241,7 +253,7 @@ frame_reset_kernel(FrameBuffers fb, BinBuffers bb, uint32_t nl_nodes, uint32_t n
             *fb.error = 0u;
             *fb.fragments = 0ull;
         }
-        if (draw) bb.large_count[0] = bb.large_count[1] = 0u;
+        if (draw) bb.large_count[0] = bb.large_count[1] = bb.large_count[2] = 0u;
     }
 }
 

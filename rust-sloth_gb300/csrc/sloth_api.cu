@@ -70,6 +70,7 @@ struct sloth_ctx {
     BinBuffers bb{};
     uint32_t ntiles_cap = 0;
     size_t large_cap = 0;
+    size_t fill_cap = 0;
     float4 *tv = nullptr;
     size_t tv_cap = 0;
     uint32_t *h_total = nullptr;   // pinned
@@ -529,6 +530,7 @@ void sloth_ctx_destroy(sloth_ctx *ctx)
     dfree(ctx->fb.rows);
     dfree(ctx->bb.entries);
     dfree(ctx->bb.large_queue);
+    dfree(ctx->bb.fill_list);
     dfree(ctx->bb.large_count);
     dfree(ctx->bb.items);
     dfree(ctx->tv);
@@ -883,7 +885,8 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     if ((st = ensure_records(ctx, (size_t)ctx->tri_base + mesh->ntri)) != SLOTH_OK) return st;
     if (mesh->idx && (st = ensure_scratch(ctx, &ctx->tv, &ctx->tv_cap, mesh->nvert)) != SLOTH_OK) return st;
     if ((st = ensure_scratch(ctx, &ctx->bb.large_queue, &ctx->large_cap, mesh->ntri)) != SLOTH_OK) return st;
-    if (!ctx->bb.large_count) CU(ctx, dalloc(&ctx->bb.large_count, 2));
+    if ((st = ensure_scratch(ctx, &ctx->bb.fill_list, &ctx->fill_cap, mesh->ntri)) != SLOTH_OK) return st;
+    if (!ctx->bb.large_count) CU(ctx, dalloc(&ctx->bb.large_count, 3));
     ctx->bb.large_cap = mesh->ntri;
 
     Mat4 M;
@@ -924,7 +927,7 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
                       ctx->aux));
         CU(ctx, cudaEventRecord(ctx->aux_ev, ctx->aux));
         CU(ctx, timed(ctx, "bin_fill", [&] {
-               return launch_bin_fill(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->bb, s, ctx->tpb);
+               return launch_bin_fill(ctx->tri_base, g, ctx->fb, ctx->bb, s);
            }));
         CU(ctx, cudaStreamWaitEvent(s, ctx->aux_ev, 0));
         size_t icap = ctx->bb.item_capacity;

@@ -81,6 +81,17 @@ struct __align__(16) TriRecord {
 };
 static_assert(sizeof(TriRecord) == 96, "record layout");
 
+// The whole record in one round trip (six 16-byte loads).
+__device__ __forceinline__ TriRecord load_record(const TriRecord *__restrict__ recs, uint32_t i)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(recs + i);
+    TriRecord r;
+    float4 *o = reinterpret_cast<float4 *>(&r);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[k] = __ldg(p + k);
+    return r;
+}
+
 constexpr uint32_t kFlagFiniteXY = 1u;   // |x|,|y| of all vertices < 1e18: edge functions are
                                          // monotone and overflow-free, corner tests are exact
 constexpr uint32_t kFlagTight = 2u;      // xe was tightened below the reference's x bound

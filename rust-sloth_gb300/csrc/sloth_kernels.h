@@ -48,8 +48,11 @@ struct BinBuffers {
     uint32_t capacity;
     uint32_t *large_queue;   // large_cap mesh-local indices of triangles binned by warps: big
                              // ones from the front, the others from the back (bin_common.cuh)
-    uint32_t *large_count;   // 2: big triangles queued, other large triangles queued
+    uint32_t *large_count;   // 3: big triangles queued, other large triangles queued, and
+                             // (contexts) small binned triangles listed in fill_list
     uint32_t large_cap;
+    uint32_t *fill_list;     // large_cap: draw-local indices of the small binned triangles
+                             // (setup appends, the fill walks them); null: none kept
     uint32_t *slice_offset;  // ntiles + kSliceExtra: per tile the first raster item of its
                              // slices within its class (item_offset); [ntiles] = items,
                              // [ntiles+1] = split threshold, [ntiles+2] = slice size,
@@ -169,9 +172,9 @@ cudaError_t launch_bin_count_large(uint32_t tri_base, const FrameGeom &g, const 
 cudaError_t launch_bin_scan(uint32_t ntiles, const BinBuffers &bb, cudaStream_t s);
 cudaError_t launch_bin_items(uint32_t ntiles, const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
                              cudaStream_t s);
-cudaError_t launch_bin_fill(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
-                            const FrameBuffers &fb, const BinBuffers &bb, cudaStream_t s,
-                            int tpb = kDefaultTrianglesPerBlock);
+// small binned triangles' tile entries: the ones setup listed in bb.fill_list
+cudaError_t launch_bin_fill(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
+                            cudaStream_t s);
 cudaError_t launch_bin_fill_large(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
                                   const BinBuffers &bb, cudaStream_t s);
 
