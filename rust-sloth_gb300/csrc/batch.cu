@@ -89,7 +89,8 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
         large = sp.large;
     }
     const bool binned = live && !large && !direct && sp.ntiles != 0;
-    count_small_tiles_warp(binned, r, vp, sp, b.bb.tile_count + f.tile_off);
+    const uint32_t slot1 = count_small_tiles_warp(binned, r, vp, sp, b.bb.tile_count + f.tile_off,
+                                                  b.bb.tile_cursor + f.tile_off);
     // the fill's work list: one atomic per warp
     const unsigned bm = __ballot_sync(0xffffffffu, binned);
     if (bm) {
@@ -97,7 +98,7 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(b.fill_count, (uint32_t)__popc(bm));
         base = __shfl_sync(0xffffffffu, base, 0);
-        if (binned) b.fill_list[base + __popc(bm & ((1u << lane) - 1u))] = make_uint2(d.frame, d.local_base + t);
+        if (binned) b.fill_list[base + __popc(bm & ((1u << lane) - 1u))] = make_uint4(d.frame, d.local_base + t, slot1, 0u);
     }
     if (__any_sync(0xffffffffu, large)) {
         const int q = large_slot(large, sp.ntiles, b.bb.large_count, b.bb.large_cap);
@@ -240,7 +241,7 @@ __global__ void __launch_bounds__(kSetupThreads, kFillMinBlocks) batch_fill_kern
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         const bool live = i < n;
-        const uint2 e = live ? b.fill_list[i] : make_uint2(0u, 0u);
+        const uint4 e = live ? b.fill_list[i] : make_uint4(0u, 0u, 0u, 0u);
         const BatchFrame &f = b.frames[e.x];
         const Viewport vp = vp_batch(f.g);
         TriRecord r;
@@ -249,7 +250,8 @@ __global__ void __launch_bounds__(kSetupThreads, kFillMinBlocks) batch_fill_kern
             r = load_record(f.fb.records, e.y);
             sp = tile_span(vp, r);
         }
-        fill_small_warp(live, r, e.y, vp, sp, b.bb.tile_cursor, b.bb.entries, b.bb.capacity, f.tile_off);
+        fill_small_warp(live, r, e.y, vp, sp, b.bb.tile_offset, b.bb.tile_cursor, b.bb.entries, b.bb.capacity, e.z,
+                        f.tile_off);
     }
 }
 

@@ -71,7 +71,7 @@ struct sloth_batch {
     uint32_t *large_frame = nullptr;
     uint32_t *overflow = nullptr;
     uint32_t *queue = nullptr;                // the persistent raster's item counter
-    uint2 *fill_list = nullptr;               // the fill's work list (one entry per record at most)
+    uint4 *fill_list = nullptr;               // the fill's work list (one entry per record at most)
     uint32_t *fill_count = nullptr;
     uint32_t *h_total = nullptr;              // pinned
     uint32_t *h_overflow = nullptr;           // pinned
@@ -364,6 +364,7 @@ cudaError_t enqueue_front(sloth_batch *b, const BatchDev &d, cudaStream_t s)
 {
     cudaError_t e;
     if ((e = cudaMemsetAsync(b->bb.tile_count, 0, (size_t)b->total_tiles * 4, s))) return e;
+    if ((e = cudaMemsetAsync(b->bb.tile_cursor, 0, (size_t)b->total_tiles * 4, s))) return e;
     if (b->direct_max > 0) {
         // small triangles fold into the global keys during setup: every tile's keys start
         // empty and current (kBatchGen is 0x01 in every byte)

@@ -46,8 +46,9 @@ struct BatchDev {
     uint32_t *large_frame;     // frame of each large-queue entry
     uint32_t *overflow;        // set when the entries outgrew their capacity
     uint32_t *queue;           // the persistent raster's next item (zeroed by the item kernel)
-    uint2 *fill_list;          // (frame, frame-local draw index) of every small binned triangle,
-                               // appended by setup: the fill walks only these
+    uint4 *fill_list;          // (frame, frame-local draw index, slot in its first tile, 0) of
+                               // every small binned triangle, appended by setup: the fill walks
+                               // only these
     uint32_t *fill_count;      // entries of fill_list (zeroed at the start of a render)
     int depth_cull;
     int tpb;                   // triangles per setup/fill block (the triangle block table's step)

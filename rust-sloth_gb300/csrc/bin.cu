@@ -39,8 +39,10 @@ __device__ __forceinline__ SplitParams split_params(const BinBuffers &bb, uint32
     return SplitParams{bb.slice_offset[n + 1], bb.slice_offset[n + 2]};
 }
 
-// Exclusive scans of the tile entry counts (offsets, cursors; offsets[n] = total) and of
-// the raster items per tile, by one block, 4096 tiles per step with running carries.  A
+// Exclusive scans of the tile entry counts (tile_count + tile_cursor: the entries with a
+// counted slot and the others; offsets[n] = total) and of the raster items per tile, by one
+// block, 4096 tiles per step with running carries.  Afterwards tile_count holds each tile's
+// entries and tile_cursor the first slot after its counted ones.  A
 // first pass sets the split threshold and the light threshold from the mean entries of a
 // non-empty tile.  Items are numbered in three classes: split tiles' slices first (they
 // start first), then the other tiles in tile order, then light tiles (fewer entries than
@@ -62,7 +64,7 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
     unsigned long long se = 0;
     uint32_t st = 0;
     for (uint32_t i = tid; i < n; i += blockDim.x) {
-        const uint32_t c = bb.tile_count[i];
+        const uint32_t c = bb.tile_count[i] + bb.tile_cursor[i];   // first-tile and other entries
         se += c;
         st += c != 0u;
     }
@@ -99,10 +101,11 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
     // pass 2: the scans
     for (uint32_t base = 0; base < n; base += 4 * 1024) {
         const uint32_t i0 = base + 4 * tid;
-        uint32_t c[4], cls[4], loc[kV] = {0, 0, 0, 0};
+        uint32_t c[4], c1[4], cls[4], loc[kV] = {0, 0, 0, 0};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            c[k] = i0 + k < n ? bb.tile_count[i0 + k] : 0u;
+            c1[k] = i0 + k < n ? bb.tile_count[i0 + k] : 0u;
+            c[k] = c1[k] + (i0 + k < n ? bb.tile_cursor[i0 + k] : 0u);
             cls[k] = c[k] > sp.threshold ? 1u : (c[k] < light ? 3u : 2u);
             loc[0] += c[k];
             loc[cls[k]] += tile_slices(c[k], sp);
@@ -144,8 +147,11 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             if (i0 + k < n) {
+                // the first-tile entries take [offset, offset + c1) by their counted slots,
+                // the others the slots after them from the cursor
                 bb.tile_offset[i0 + k] = p[0];
-                bb.tile_cursor[i0 + k] = p[0];
+                bb.tile_cursor[i0 + k] = p[0] + c1[k];
+                bb.tile_count[i0 + k] = c[k];
                 bb.slice_offset[i0 + k] = p[cls[k]];
             }
             p[0] += c[k];
@@ -215,14 +221,15 @@ bin_fill_kernel(uint32_t tri_base, FrameGeom g, FrameBuffers fb, BinBuffers bb)
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         const bool live = i < n;
-        const uint32_t gtri = tri_base + (live ? bb.fill_list[i] : 0u);
+        const uint2 e = live ? bb.fill_list[i] : make_uint2(0u, 0u);
+        const uint32_t gtri = tri_base + e.x;
         TriRecord r;
         TileSpan sp{};
         if (live) {
             r = load_record(fb.records, gtri);
             sp = tile_span(vp, r);
         }
-        fill_small_warp(live, r, gtri, vp, sp, bb.tile_cursor, bb.entries, bb.capacity);
+        fill_small_warp(live, r, gtri, vp, sp, bb.tile_offset, bb.tile_cursor, bb.entries, bb.capacity, e.y);
     }
 }
 

@@ -69,9 +69,9 @@ __device__ __forceinline__ uint32_t large_items(const uint32_t *large_count)
     return large_count[0] * kBigParts + large_count[1];
 }
 
-// One warp walks part `part` of `nparts` of a large triangle's tile rectangles: counts (kFill false)
-// or writes its entries (kFill true), with a per-tile depth bound (tighter than the
-// triangle-wide one).
+// One warp walks part `part` of `nparts` of a large triangle's tile rectangles: counts (kFill
+// false, in tile_cursor: entries whose slots come from the cursor after the scan) or writes
+// its entries (kFill true), with a per-tile depth bound (tighter than the triangle-wide one).
 // The sample range (16 bytes) decides first whether the part has tiles at all; only then
 // is the whole record read.
 template <bool kFill>
@@ -113,51 +113,44 @@ __device__ __forceinline__ void bin_large_warp(const TriRecord *rec, uint32_t gt
             const uint32_t slot = atomicAdd(&tile_cursor[tile], 1u);
             if (slot < capacity) entries[slot] = entry_key(zlo, gtri, !cw.empty());
         } else {
-            atomicAdd(&tile_count[tile], 1u);
+            // counted among the tile's entries without a slot: the cursor array holds those
+            // counts until the scan (count_small_tiles_warp)
+            atomicAdd(&tile_cursor[tile], 1u);
         }
     }
 }
 
-// Writes a small triangle's entries.  Called by all 32 lanes (lanes with active false
-// write nothing); each lane's first tile takes its slots with one atomic per distinct
-// tile of the warp, like count_small_tiles_warp.  A lane's tiles are tile_base + the
-// frame-local index in tile_cursor (lanes of one warp may belong to different frames).
+// Writes a small triangle's entries: the one in its first tile at the slot the count pass
+// gave it (slot1, after the tile's first tile_offset), the others at slots taken from the
+// tiles' cursors.  A lane's tiles are tile_base + the frame-local index (the lanes of one
+// warp may belong to different frames).
 __device__ __forceinline__ void fill_small_warp(bool active, const TriRecord &r, uint32_t gtri, const Viewport &vp,
-                                                const TileSpan &sp, uint32_t *tile_cursor, uint64_t *entries,
-                                                uint32_t capacity, uint32_t tile_base = 0)
+                                                const TileSpan &sp, const uint32_t *tile_offset,
+                                                uint32_t *tile_cursor, uint64_t *entries, uint32_t capacity,
+                                                uint32_t slot1, uint32_t tile_base = 0)
 {
-    uint32_t first = 0xffffffffu;
-    bool first_wrapped = false;
-    if (active) {
-        auto put = [&](int tr, int tc) {
-            const bool wrapped = !sp.W.empty() && !clip_wrapped(vp, sp.W, tr, tc).empty();
-            const uint32_t tile = tile_base + tr * vp.ntx + tc;
-            if (first == 0xffffffffu) {
-                first = tile;
-                first_wrapped = wrapped;
-                return;
-            }
-            const uint32_t slot = atomicAdd(&tile_cursor[tile], 1u);
-            if (slot < capacity) entries[slot] = entry_key(r.zlo, gtri, wrapped);
-        };
-        for (int tr = sp.TU.ya; tr < sp.TU.yb; ++tr)
-            for (int tc = sp.TU.xa; tc < sp.TU.xb; ++tc)
-                if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
-        for (int tr = sp.TW.ya; tr < sp.TW.yb; ++tr)
-            for (int tc = sp.TW.xa; tc < sp.TW.xb; ++tc) {
-                if (in_rect(sp.TU, tr, tc)) continue;
-                if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
-            }
-    }
-    const unsigned peers = __match_any_sync(0xffffffffu, first);
-    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
-    uint32_t base = 0;
-    if (first != 0xffffffffu && lane == leader) base = atomicAdd(&tile_cursor[first], (uint32_t)__popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (first != 0xffffffffu) {
-        const uint32_t slot = base + __popc(peers & ((1u << lane) - 1u));
-        if (slot < capacity) entries[slot] = entry_key(r.zlo, gtri, first_wrapped);
-    }
+    if (!active) return;
+    bool first = true;
+    auto put = [&](int tr, int tc) {
+        const bool wrapped = !sp.W.empty() && !clip_wrapped(vp, sp.W, tr, tc).empty();
+        const uint32_t tile = tile_base + tr * vp.ntx + tc;
+        uint32_t slot;
+        if (first) {
+            slot = tile_offset[tile] + slot1;
+            first = false;
+        } else {
+            slot = atomicAdd(&tile_cursor[tile], 1u);
+        }
+        if (slot < capacity) entries[slot] = entry_key(r.zlo, gtri, wrapped);
+    };
+    for (int tr = sp.TU.ya; tr < sp.TU.yb; ++tr)
+        for (int tc = sp.TU.xa; tc < sp.TU.xb; ++tc)
+            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
+    for (int tr = sp.TW.ya; tr < sp.TW.yb; ++tr)
+        for (int tc = sp.TW.xa; tc < sp.TW.xb; ++tc) {
+            if (in_rect(sp.TU, tr, tc)) continue;
+            if (tile_hit(r, vp, sp.U, sp.W, tr, tc)) put(tr, tc);
+        }
 }
 
 }  // namespace sloth

@@ -305,19 +305,22 @@ __device__ __forceinline__ float4 transform_vertex(const MeshDev &mesh, const Ma
     return make_float4(row_dot(&M.m[0], x, y, z), row_dot(&M.m[4], x, y, z), row_dot(&M.m[8], x, y, z), 0.0f);
 }
 
-// Count the small triangle's tiles (bin count pass).
-// Adds 1 to the count of every tile a small triangle can write.  Called by all 32 lanes
-// (lanes with active false count nothing).  Each lane's first tile is counted with one
-// atomic per distinct tile of the warp: consecutive triangles of a mesh mostly share it.
-__device__ __forceinline__ void count_small_tiles_warp(bool active, const TriRecord &r, const Viewport &vp,
-                                                       const TileSpan &sp, uint32_t *tile_count)
+// Counts the small triangle's tiles (bin count pass) and returns the triangle's slot among
+// the entries of its first tile.  A triangle's first tile (the first tile_hit in the loop
+// order below, which fill_small_warp repeats) is counted in tile_count with one atomic per
+// distinct tile of the warp, whose returned value gives each lane its slot; its other
+// tiles are counted in tile_extra without a slot (the fill takes theirs from the tile's
+// cursor).  Called by all 32 lanes (lanes with active false count nothing and get 0).
+__device__ __forceinline__ uint32_t count_small_tiles_warp(bool active, const TriRecord &r, const Viewport &vp,
+                                                           const TileSpan &sp, uint32_t *tile_count,
+                                                           uint32_t *tile_extra)
 {
     uint32_t first = 0xffffffffu;
     if (active) {
         auto hit = [&](int tr, int tc) {
             const uint32_t tile = tr * vp.ntx + tc;
             if (first == 0xffffffffu) first = tile;
-            else atomicAdd(&tile_count[tile], 1u);
+            else atomicAdd(&tile_extra[tile], 1u);
         };
         for (int tr = sp.TU.ya; tr < sp.TU.yb; ++tr)
             for (int tc = sp.TU.xa; tc < sp.TU.xb; ++tc)
@@ -329,8 +332,11 @@ __device__ __forceinline__ void count_small_tiles_warp(bool active, const TriRec
             }
     }
     const unsigned peers = __match_any_sync(0xffffffffu, first);
-    if (first != 0xffffffffu && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
-        atomicAdd(&tile_count[first], (uint32_t)__popc(peers));
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (first != 0xffffffffu && lane == leader) base = atomicAdd(&tile_count[first], (uint32_t)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return first != 0xffffffffu ? base + (uint32_t)__popc(peers & ((1u << lane) - 1u)) : 0u;
 }
 
 }  // namespace sloth

@@ -97,7 +97,7 @@ __device__ __forceinline__ void setup_triangle(uint32_t tri_base, const FrameGeo
     // binning: count tiles of small triangles here and list them for the fill, queue the
     // rest for warps
     const bool binned = live && !large && !direct && sp.ntiles != 0;
-    count_small_tiles_warp(binned, r, vp, sp, bb.tile_count);
+    const uint32_t slot1 = count_small_tiles_warp(binned, r, vp, sp, bb.tile_count, bb.tile_cursor);
     if (bb.fill_list) {
         const unsigned bm = __ballot_sync(0xffffffffu, binned);
         if (bm) {
@@ -105,7 +105,7 @@ __device__ __forceinline__ void setup_triangle(uint32_t tri_base, const FrameGeo
             uint32_t first = 0;
             if (lane == 0) first = atomicAdd(&bb.large_count[2], (uint32_t)__popc(bm));
             first = __shfl_sync(0xffffffffu, first, 0);
-            if (binned) bb.fill_list[first + __popc(bm & ((1u << lane) - 1u))] = t;
+            if (binned) bb.fill_list[first + __popc(bm & ((1u << lane) - 1u))] = make_uint2(t, slot1);
         }
     }
     // warp-ballot compaction of the large-triangle queue
@@ -246,7 +246,7 @@ frame_reset_kernel(FrameBuffers fb, BinBuffers bb, uint32_t nl_nodes, uint32_t n
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (frame && i < nl_nodes) fb.nltree[i] = -1;
-    if (draw && i < ntiles) bb.tile_count[i] = 0u;
+    if (draw && i < ntiles) bb.tile_count[i] = bb.tile_cursor[i] = 0u;
     if (tiles_current && i < ntiles) fb.tile_gen[i] = fb.gen;
     if (i == 0) {
         if (frame) {

@@ -41,9 +41,12 @@ struct FrameBuffers {
 
 // Binning scratch of one draw.
 struct BinBuffers {
-    uint32_t *tile_count;    // ntiles
+    uint32_t *tile_count;    // ntiles: before the scan the entries of small triangles whose
+                             // first tile it is (each with its slot from the count), after it
+                             // all the tile's entries
     uint32_t *tile_offset;   // ntiles + 1 (exclusive scan; [ntiles] = total entries)
-    uint32_t *tile_cursor;   // ntiles
+    uint32_t *tile_cursor;   // ntiles: before the scan the tile's other entries (counted without
+                             // a slot), after it the next of their slots
     uint64_t *entries;       // capacity: per tile, (ordered depth lower bound << 32 | draw index)
     uint32_t capacity;
     uint32_t *large_queue;   // large_cap mesh-local indices of triangles binned by warps: big
@@ -51,8 +54,9 @@ struct BinBuffers {
     uint32_t *large_count;   // 3: big triangles queued, other large triangles queued, and
                              // (contexts) small binned triangles listed in fill_list
     uint32_t large_cap;
-    uint32_t *fill_list;     // large_cap: draw-local indices of the small binned triangles
-                             // (setup appends, the fill walks them); null: none kept
+    uint2 *fill_list;        // large_cap: (draw-local index, slot in its first tile) of the
+                             // small binned triangles (setup appends, the fill walks them);
+                             // null: none kept
     uint32_t *slice_offset;  // ntiles + kSliceExtra: per tile the first raster item of its
                              // slices within its class (item_offset); [ntiles] = items,
                              // [ntiles+1] = split threshold, [ntiles+2] = slice size,
