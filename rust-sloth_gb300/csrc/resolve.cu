@@ -9,7 +9,7 @@ namespace sloth {
 constexpr int kRun = 2;
 constexpr int kEvenPairs = 4;
 
-__global__ void __launch_bounds__(256) resolve_kernel(FrameGeom g, FrameBuffers fb, int vec)
+__global__ void __launch_bounds__(256, 4) resolve_kernel(FrameGeom g, FrameBuffers fb, int vec)
 {
     const uint64_t nz = (uint64_t)g.w * g.h;
     const uint64_t ncells = g.image ? nz + g.h : nz;
@@ -33,7 +33,7 @@ cudaError_t launch_resolve(const FrameGeom &g, const FrameBuffers &fb, cudaStrea
     if (ncells == 0) return cudaSuccess;
     const uint64_t per_block = 256ull * kRun * ((g.w & 1) ? 1 : kEvenPairs);   // cells
     uint64_t blocks = (ncells + per_block - 1) / per_block;
-    const uint64_t cap = 32ull * (uint64_t)device_sm_count();   // eight resident CTAs per SM, four waves
+    const uint64_t cap = 32ull * (uint64_t)device_sm_count();   // four resident CTAs per SM (64 registers), eight waves
     if (blocks > cap) blocks = cap;
     const int vec = ((reinterpret_cast<uintptr_t>(fb.cells_out) | reinterpret_cast<uintptr_t>(fb.z_out) |
                       reinterpret_cast<uintptr_t>(fb.winner_out)) & (4u * kRun - 1u)) == 0;
