@@ -49,6 +49,25 @@ __device__ __forceinline__ SplitParams split_params(const BinBuffers &bb, uint32
 // a quarter of the mean: mostly the frame's nearly empty borders) last, so that the last
 // wave of a launch is made of short CTAs.  slice_offset[t] is the tile's first item within
 // its class; item_offset() adds the class base.
+// The counted (tile_count) and other (tile_cursor) entries of tiles i0..i0+3, 0 past n;
+// 16-byte loads when all four exist (i0 is a multiple of 4 and the arrays 16-byte aligned).
+__device__ __forceinline__ void load_counts4(const BinBuffers &bb, uint32_t n, uint32_t i0, uint32_t c1[4],
+                                             uint32_t c2[4])
+{
+    if (i0 + 4 <= n) {
+        const uint4 a = *reinterpret_cast<const uint4 *>(bb.tile_count + i0);
+        const uint4 b = *reinterpret_cast<const uint4 *>(bb.tile_cursor + i0);
+        c1[0] = a.x; c1[1] = a.y; c1[2] = a.z; c1[3] = a.w;
+        c2[0] = b.x; c2[1] = b.y; c2[2] = b.z; c2[3] = b.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            c1[k] = i0 + k < n ? bb.tile_count[i0 + k] : 0u;
+            c2[k] = i0 + k < n ? bb.tile_cursor[i0 + k] : 0u;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers bb)
 {
     constexpr int kV = 4;   // running sums: entries, split items, other items, light items
@@ -60,13 +79,24 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
     __shared__ uint32_t light_s;
     const uint32_t tid = threadIdx.x;
     const int lane = tid & 31, wid = tid >> 5;
-    // pass 1: entries and non-empty tiles
+    // pass 1: entries and non-empty tiles, four consecutive tiles per thread and step as in
+    // pass 2; the first step's counts stay in registers for pass 2
     unsigned long long se = 0;
     uint32_t st = 0;
-    for (uint32_t i = tid; i < n; i += blockDim.x) {
-        const uint32_t c = bb.tile_count[i] + bb.tile_cursor[i];   // first-tile and other entries
-        se += c;
-        st += c != 0u;
+    uint32_t c1_0[4], c2_0[4];
+    for (uint32_t base = 0; base < n; base += 4 * 1024) {
+        uint32_t c1[4], c2[4];
+        load_counts4(bb, n, base + 4 * tid, c1, c2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (base == 0) {
+                c1_0[k] = c1[k];
+                c2_0[k] = c2[k];
+            }
+            const uint32_t c = c1[k] + c2[k];   // counted and other entries
+            se += c;
+            st += c != 0u;
+        }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -101,11 +131,19 @@ __global__ void __launch_bounds__(1024) bin_scan_kernel(uint32_t n, BinBuffers b
     // pass 2: the scans
     for (uint32_t base = 0; base < n; base += 4 * 1024) {
         const uint32_t i0 = base + 4 * tid;
-        uint32_t c[4], c1[4], cls[4], loc[kV] = {0, 0, 0, 0};
+        uint32_t c[4], c1[4], c2[4], cls[4], loc[kV] = {0, 0, 0, 0};
+        if (base == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                c1[k] = c1_0[k];
+                c2[k] = c2_0[k];
+            }
+        } else {
+            load_counts4(bb, n, i0, c1, c2);
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            c1[k] = i0 + k < n ? bb.tile_count[i0 + k] : 0u;
-            c[k] = c1[k] + (i0 + k < n ? bb.tile_cursor[i0 + k] : 0u);
+            c[k] = c1[k] + c2[k];
             cls[k] = c[k] > sp.threshold ? 1u : (c[k] < light ? 3u : 2u);
             loc[0] += c[k];
             loc[cls[k]] += tile_slices(c[k], sp);
