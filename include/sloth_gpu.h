@@ -181,9 +181,9 @@ sloth_status sloth_ctx_flush_device(sloth_ctx *ctx, int format, const char **dev
  *   takes effect at the next sloth_ctx_clear.  Results are identical either way. */
 #define SLOTH_OPTION_DIRECT_SAMPLES 4
 #define SLOTH_MAX_DIRECT_SAMPLES 256
-/* SLOTH_OPTION_TRIANGLES_PER_BLOCK: triangles per block of the setup and fill kernels,
- *   128, 256 (the default), 1024 or 4096; a block has at most 256 threads, each taking its
- *   share of the block's triangles in turn.  Results are identical either way. */
+/* SLOTH_OPTION_TRIANGLES_PER_BLOCK: triangles per block of the setup kernel, 128, 256 (the
+ *   default), 1024 or 4096; a block has at most 256 threads, each taking its share of the
+ *   block's triangles in turn.  Results are identical either way. */
 #define SLOTH_OPTION_TRIANGLES_PER_BLOCK 5
 sloth_status sloth_ctx_set_option(sloth_ctx *ctx, int option, int64_t value);
 
@@ -288,7 +288,7 @@ sloth_status sloth_batch_set_persistent(sloth_batch *batch, int persistent);
 /* Rasterize triangles of at most `samples` samples straight into the depth keys during
  * setup (SLOTH_OPTION_DIRECT_SAMPLES for a batch; a new batch takes its context's value). */
 sloth_status sloth_batch_set_direct_samples(sloth_batch *batch, int samples);
-/* Triangles per block of the batch's setup and fill kernels (SLOTH_OPTION_TRIANGLES_PER_BLOCK):
+/* Triangles per block of the batch's setup kernel (SLOTH_OPTION_TRIANGLES_PER_BLOCK):
  * 128, 256 (the default), 1024 or 4096. */
 sloth_status sloth_batch_set_triangles_per_block(sloth_batch *batch, int tpb);
 /* Autotuner: times `reps` renders of the batch per candidate setting and keeps the fastest

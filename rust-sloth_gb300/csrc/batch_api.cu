@@ -35,7 +35,7 @@ struct sloth_batch {
     int shape = 0;
     int direct_max = 0;                       // FrameGeom::direct_max of every frame
     bool persistent = true;                   // raster over the device queue (else one CTA per item)
-    int tpb = kDefaultTrianglesPerBlock;      // triangles per setup/fill block
+    int tpb = kDefaultTrianglesPerBlock;      // triangles per setup block
 
     // layout (per shape)
     std::vector<BatchFrame> hframes;

@@ -51,7 +51,7 @@ struct BatchDev {
                                // only these
     uint32_t *fill_count;      // entries of fill_list (zeroed at the start of a render)
     int depth_cull;
-    int tpb;                   // triangles per setup/fill block (the triangle block table's step)
+    int tpb;                   // triangles per setup block (the triangle block table's step)
     int direct_max;            // the frames' FrameGeom::direct_max (the same for every frame)
 };
 

@@ -117,10 +117,11 @@ struct Mat4 {
     float m[16];             // row-major
 };
 
-// Triangles per block of the setup and fill kernels: a tuning choice, the results do not
-// depend on it.  A block has min(tpb, kSetupThreads) threads, and each thread takes
-// tpb / threads triangles in turn (consecutive threads, consecutive triangles), so that a
-// triangle's record stores and key reductions drain while the thread sets up the next.
+// Triangles per block of the setup kernels: a tuning choice, the results do not depend on
+// it.  A block has min(tpb, kSetupThreads) threads, and each thread takes tpb / threads
+// triangles in turn (consecutive threads, consecutive triangles), so that a triangle's
+// record stores and key reductions drain while the thread sets up the next.  The fills walk
+// the list setup made, a grid of kFillMinBlocks * 2 blocks per SM.
 constexpr int kSetupThreads = 256;
 constexpr int kSetupMinBlocks = 3;   // resident setup blocks per SM the register budget keeps (direct path)
 constexpr int kFillMinBlocks = 4;    // the same for the fill kernels and setup without the direct path

@@ -268,7 +268,7 @@ class Context:
         self._check(self.lib.sloth_ctx_set_option(self.h, OPTION_DIRECT_SAMPLES, samples))
 
     def set_triangles_per_block(self, tpb: int):
-        """SLOTH_OPTION_TRIANGLES_PER_BLOCK: 128, 256, 1024 or 4096 triangles per setup/fill block."""
+        """SLOTH_OPTION_TRIANGLES_PER_BLOCK: 128, 256, 1024 or 4096 triangles per setup block."""
         self._check(self.lib.sloth_ctx_set_option(self.h, OPTION_TRIANGLES_PER_BLOCK, tpb))
 
     def autotune(self, draws, reps: int = 3) -> dict:
