@@ -129,7 +129,10 @@ __device__ __forceinline__ bool needs_setup(float4 p1, float4 p2, float4 p3, int
     const float big = 1e18f;
     const bool finite = fabsf(p1.x) < big && fabsf(p1.y) < big && fabsf(p2.x) < big &&
                         fabsf(p2.y) < big && fabsf(p3.x) < big && fabsf(p3.y) < big;
-    if (finite && provably_empty(orient_bound(r))) {
+    // the proof needs o < -err with err >= 0: a triangle whose computed orient o (the value
+    // orient_bound computes first) is not negative is never proven empty, so the bound is
+    // worked out only for the others (back faces, mostly)
+    if (finite && edge_eval(r.dx2, r.dy2, r.v1x, r.v1y, r.v3x, r.v3y) < 0.0f && provably_empty(orient_bound(r))) {
         row4 = make_int4(r.x0, r.x0, r.y0, r.y1);
         return false;
     }
