@@ -49,20 +49,15 @@ __global__ void __launch_bounds__(256) batch_vertex_kernel(BatchDev b, const int
                                      row_dot(&M.m[8], xs[k], ys[k], zs[k]), 0.0f);
 }
 
-// The three vertices of triangle t of draw d transformed by the draw's matrix M in place
-// (the vertex kernel's operations): a mesh shared by many views stays in L2, and no
-// transformed-vertex buffer is written and read back for the render.
-__device__ __forceinline__ void batch_triangle_vertices(const BatchDraw &d, const Mat4 &M, uint32_t t, float4 &p1,
-                                                        float4 &p2, float4 &p3)
+// The three vertices of triangle t of draw d, at position p of setup's order of the mesh,
+// transformed by the draw's matrix M in place (the vertex kernel's operations): a mesh
+// shared by many views stays in L2, and no transformed-vertex buffer is written and read
+// back for the render.
+__device__ __forceinline__ void batch_triangle_vertices(const BatchDraw &d, const Mat4 &M, uint32_t p, uint32_t t,
+                                                        float4 &p1, float4 &p2, float4 &p3)
 {
     uint32_t i1, i2, i3;
-    if (d.mesh.idx) {
-        i1 = __ldg(d.mesh.idx + 3 * (size_t)t + 0);
-        i2 = __ldg(d.mesh.idx + 3 * (size_t)t + 1);
-        i3 = __ldg(d.mesh.idx + 3 * (size_t)t + 2);
-    } else {
-        i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
-    }
+    mesh_corners(d.mesh, p, t, i1, i2, i3);
     p1 = transform_vertex(d.mesh, M, i1);
     p2 = transform_vertex(d.mesh, M, i2);
     p3 = transform_vertex(d.mesh, M, i3);
@@ -85,7 +80,9 @@ __device__ __forceinline__ void batch_setup_triangle(const BatchDev &b, const Ba
         r = build_record(p1, p2, p3, rgb, f.g.w, f.g.h, kDirect ? f.g.direct_max : 0, kDirect ? &dw : nullptr);
         direct = dw.direct;
         if (!direct) sp = tile_span(vp, r);   // a direct triangle is not binned
-        store_record(f.fb.records + d.local_base + t, r, sp.ntiles, direct);
+        // a triangle with nothing to rasterize is never read back here (the fill walks the
+        // fill list, the newline the packed rows): its record is not written
+        if (direct || sp.ntiles != 0) store_record(f.fb.records + d.local_base + t, r, sp.ntiles, direct);
         large = sp.large;
     }
     const bool binned = live && !large && !direct && sp.ntiles != 0;
@@ -145,28 +142,30 @@ __global__ void __launch_bounds__(kSetupThreads, kDirect ? kSetupMinBlocks : kFi
     for (uint32_t c0 = t0; c0 < t_end; c0 += cap) {
         // two triangles per round, their vertex loads issued together (the same trip count
         // in every lane)
-        for (uint32_t t = c0 + threadIdx.x; t < c0 + cap; t += 2 * blockDim.x) {
-            const uint32_t u = t + blockDim.x;
-            const bool lt = t < t_end, lu = u < c0 + cap && u < t_end;
+        // (positions p and q of setup's order: triangles tp and tq; the packed rows are
+        // stored by position, everything else by triangle)
+        for (uint32_t p = c0 + threadIdx.x; p < c0 + cap; p += 2 * blockDim.x) {
+            const uint32_t q = p + blockDim.x;
+            const bool lt = p < t_end, lu = q < c0 + cap && q < t_end;
             float4 a1, a2, a3, b1, b2, b3;
-            uint32_t ca = 0, cb = 0;
+            uint32_t ca = 0, cb = 0, tp = 0, tq = 0;
             if (lt) {
-                batch_triangle_vertices(d, sm, t, a1, a2, a3);
-                ca = load_rgb(d.mesh.rgb, t);
+                tp = mesh_triangle(d.mesh, p);
+                batch_triangle_vertices(d, sm, p, tp, a1, a2, a3);
+                ca = load_rgb(d.mesh.rgb, tp);
             }
             if (lu) {
-                batch_triangle_vertices(d, sm, u, b1, b2, b3);
-                cb = load_rgb(d.mesh.rgb, u);
+                tq = mesh_triangle(d.mesh, q);
+                batch_triangle_vertices(d, sm, q, tq, b1, b2, b3);
+                cb = load_rgb(d.mesh.rgb, tq);
             }
             int4 row4;
             const bool kt = lt && needs_setup(a1, a2, a3, f.g.w, f.g.h, row4);
-            if (lt && !kt) store_row4(f.fb.records + d.local_base + t, row4);
-            if (lt) f.fb.rows[d.local_base + t] = pack_rows(row4.z, row4.w);
-            stash_push(st, &sq_n, base, kt, t, a1, a2, a3, ca);
+            if (lt) f.fb.rows[d.local_base + p] = pack_rows(row4.z, row4.w);
+            stash_push(st, &sq_n, base, kt, tp, a1, a2, a3, ca);
             const bool ku = lu && needs_setup(b1, b2, b3, f.g.w, f.g.h, row4);
-            if (lu && !ku) store_row4(f.fb.records + d.local_base + u, row4);
-            if (lu) f.fb.rows[d.local_base + u] = pack_rows(row4.z, row4.w);
-            stash_push(st, &sq_n, base, ku, u, b1, b2, b3, cb);
+            if (lu) f.fb.rows[d.local_base + q] = pack_rows(row4.z, row4.w);
+            stash_push(st, &sq_n, base, ku, tq, b1, b2, b3, cb);
         }
         block_sync();
         const uint32_t total = sq_n, nq = total - base;
@@ -200,9 +199,9 @@ __global__ void __launch_bounds__(1024) batch_newline_kernel(BatchDev b, const i
         block_sync();
     }
     const uint32_t lo = (uint32_t)blk.y, hi = min(d.mesh.ntri, lo + kBatchNewlineChunk);
-    for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
-        const int32_t v = (int32_t)(d.local_base + t);
-        const uint32_t yr = __ldg(f.fb.rows + d.local_base + t);
+    for (uint32_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+        const int32_t v = (int32_t)(d.local_base + mesh_triangle(d.mesh, p));
+        const uint32_t yr = __ldg(f.fb.rows + d.local_base + p);
         nltree_update(tree, n, (int)(yr & 0xffffu), (int)(yr >> 16), v, kShared);
     }
     if (kShared) {

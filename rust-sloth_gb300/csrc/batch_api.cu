@@ -112,6 +112,7 @@ struct MeshView {
     const uint8_t *rgb;
     uint32_t nvert, ntri;
     int device;
+    const uint32_t *order, *oidx;   // setup's order of an indexed mesh (MeshDev), or null
 };
 MeshView sloth_mesh_view(const sloth_mesh *m);
 }
@@ -252,7 +253,7 @@ sloth_status build(sloth_batch *b, int shape)
             const uint32_t d = fd.first_draw + k;
             const MeshView mv = sloth_mesh_view(b->meshes[d]);
             BatchDraw &bd = hd[d];
-            bd.mesh = MeshDev{mv.x, mv.y, mv.z, mv.idx, mv.rgb, mv.nvert, mv.ntri};
+            bd.mesh = MeshDev{mv.x, mv.y, mv.z, mv.idx, mv.rgb, mv.nvert, mv.ntri, mv.order, mv.oidx};
             bd.frame = f;
             bd.rec_off = (uint32_t)(rec + local);
             bd.local_base = local;

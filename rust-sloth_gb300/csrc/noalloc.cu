@@ -205,7 +205,7 @@ extern "C" sloth_status sloth_render_noalloc(const float *x, const float *y, con
     for (int i = 0; i < 16; ++i) M.m[i] = m[i];
     MeshDev md{x, y, z, nullptr, rgb, 3 * ntri, ntri};
     if (launch_setup(md, nullptr, M, 0, g, fb, bb, s) != cudaSuccess) return SLOTH_ERR_CUDA;
-    if (launch_newline(ntri, 0, g, fb, s) != cudaSuccess) return SLOTH_ERR_CUDA;
+    if (launch_newline(ntri, nullptr, 0, g, fb, s) != cudaSuccess) return SLOTH_ERR_CUDA;
     if (ntri) {
         noalloc_raster_kernel<<<ntiles, 256, 0, s>>>(ntri, g, fb);
         if (cudaGetLastError() != cudaSuccess) return SLOTH_ERR_CUDA;

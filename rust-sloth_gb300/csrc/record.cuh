@@ -301,6 +301,26 @@ __device__ __forceinline__ float row_dot(const float *m, float x, float y, float
     return acc;
 }
 
+// The triangle at position p of setup's order of the mesh (MeshDev::order).
+__device__ __forceinline__ uint32_t mesh_triangle(const MeshDev &mesh, uint32_t p)
+{
+    return mesh.order ? __ldg(mesh.order + p) : p;
+}
+
+// The vertex indices of triangle t, at position p of setup's order.
+__device__ __forceinline__ void mesh_corners(const MeshDev &mesh, uint32_t p, uint32_t t, uint32_t &i1, uint32_t &i2,
+                                             uint32_t &i3)
+{
+    const uint32_t *ix = mesh.oidx ? mesh.oidx + 3 * (size_t)p : mesh.idx ? mesh.idx + 3 * (size_t)t : nullptr;
+    if (ix) {
+        i1 = __ldg(ix + 0);
+        i2 = __ldg(ix + 1);
+        i3 = __ldg(ix + 2);
+    } else {
+        i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
+    }
+}
+
 // One vertex transformed in place: (M*v).xyz with the vertex kernels' operations.
 __device__ __forceinline__ float4 transform_vertex(const MeshDev &mesh, const Mat4 &M, uint32_t i)
 {

@@ -53,19 +53,14 @@ __device__ __forceinline__ Viewport to_vp(const FrameGeom &g)
     return Viewport{g.w, g.h, g.image, g.tw, g.th, g.ntx, g.nty, g.pitch};
 }
 
-// The three transformed vertices of triangle t.  tv null (soups): the thread transforms
-// them itself, which saves the vertex kernel and its round trip through memory.
+// The three transformed vertices of triangle t, at position p of setup's order.  tv null
+// (soups): the thread transforms them itself, which saves the vertex kernel and its round
+// trip through memory.
 __device__ __forceinline__ void triangle_vertices(const MeshDev &mesh, const float4 *__restrict__ tv, const Mat4 &M,
-                                                  uint32_t t, float4 &p1, float4 &p2, float4 &p3)
+                                                  uint32_t p, uint32_t t, float4 &p1, float4 &p2, float4 &p3)
 {
     uint32_t i1, i2, i3;
-    if (mesh.idx) {
-        i1 = __ldg(mesh.idx + 3 * (size_t)t + 0);
-        i2 = __ldg(mesh.idx + 3 * (size_t)t + 1);
-        i3 = __ldg(mesh.idx + 3 * (size_t)t + 2);
-    } else {
-        i1 = 3 * t + 0; i2 = 3 * t + 1; i3 = 3 * t + 2;
-    }
+    mesh_corners(mesh, p, t, i1, i2, i3);
     if (tv) {
         p1 = __ldg(tv + i1); p2 = __ldg(tv + i2); p3 = __ldg(tv + i3);
     } else {
@@ -147,28 +142,32 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
     for (uint32_t c0 = t0; c0 < t_end; c0 += cap) {
         // two triangles per round, their vertex loads issued together (the trip count is
         // the same in every lane: cap is a multiple of twice the block size or equals it)
-        for (uint32_t t = c0 + threadIdx.x; t < c0 + cap; t += 2 * blockDim.x) {
-            const uint32_t u = t + blockDim.x;
-            const bool lt = t < t_end, lu = u < c0 + cap && u < t_end;
+        // (positions p and q of setup's order: triangles tp and tq; the packed rows are
+        // stored by position, everything else by triangle)
+        for (uint32_t p = c0 + threadIdx.x; p < c0 + cap; p += 2 * blockDim.x) {
+            const uint32_t q = p + blockDim.x;
+            const bool lt = p < t_end, lu = q < c0 + cap && q < t_end;
             float4 a1, a2, a3, b1, b2, b3;
-            uint32_t ca = 0, cb = 0;
+            uint32_t ca = 0, cb = 0, tp = 0, tq = 0;
             if (lt) {
-                triangle_vertices(mesh, tv, M, t, a1, a2, a3);
-                ca = load_rgb(mesh.rgb, t);
+                tp = mesh_triangle(mesh, p);
+                triangle_vertices(mesh, tv, M, p, tp, a1, a2, a3);
+                ca = load_rgb(mesh.rgb, tp);
             }
             if (lu) {
-                triangle_vertices(mesh, tv, M, u, b1, b2, b3);
-                cb = load_rgb(mesh.rgb, u);
+                tq = mesh_triangle(mesh, q);
+                triangle_vertices(mesh, tv, M, q, tq, b1, b2, b3);
+                cb = load_rgb(mesh.rgb, tq);
             }
             int4 row4;
             const bool kt = lt && needs_setup(a1, a2, a3, g.w, g.h, row4);
-            if (lt && !kt) store_row4(fb.records + tri_base + t, row4);
-            if (lt) fb.rows[tri_base + t] = pack_rows(row4.z, row4.w);
-            stash_push(st, &sq_n, base, kt, t, a1, a2, a3, ca);
+            if (lt && !kt) store_row4(fb.records + tri_base + tp, row4);
+            if (lt) fb.rows[tri_base + p] = pack_rows(row4.z, row4.w);
+            stash_push(st, &sq_n, base, kt, tp, a1, a2, a3, ca);
             const bool ku = lu && needs_setup(b1, b2, b3, g.w, g.h, row4);
-            if (lu && !ku) store_row4(fb.records + tri_base + u, row4);
-            if (lu) fb.rows[tri_base + u] = pack_rows(row4.z, row4.w);
-            stash_push(st, &sq_n, base, ku, u, b1, b2, b3, cb);
+            if (lu && !ku) store_row4(fb.records + tri_base + tq, row4);
+            if (lu) fb.rows[tri_base + q] = pack_rows(row4.z, row4.w);
+            stash_push(st, &sq_n, base, ku, tq, b1, b2, b3, cb);
         }
         block_sync();
         const uint32_t total = sq_n, nq = total - base;
@@ -193,10 +192,12 @@ setup_kernel(MeshDev mesh, const float4 *__restrict__ tv, Mat4 M, uint32_t tri_b
 // O(log h) node updates (canonical decomposition); a row's value is the maximum over its
 // leaf-to-root path.  Each block builds a tree for a chunk of triangles in shared memory,
 // then merges its non-empty nodes into the frame's tree.  The rows come from the packed
-// array setup wrote (4 bytes a triangle, read in order), not from the records' row 4.
+// array setup wrote (4 bytes a triangle, read in setup's order: order maps a position to
+// its triangle), not from the records' row 4.
 template <bool kShared>
 __global__ void __launch_bounds__(1024)
-newline_kernel(uint32_t ntri, uint32_t tri_base, uint32_t chunk, FrameGeom g, FrameBuffers fb)
+newline_kernel(uint32_t ntri, const uint32_t *__restrict__ order, uint32_t tri_base, uint32_t chunk, FrameGeom g,
+               FrameBuffers fb)
 {
     extern __shared__ int32_t stree[];
     const int n = g.nl_size;
@@ -206,9 +207,9 @@ newline_kernel(uint32_t ntri, uint32_t tri_base, uint32_t chunk, FrameGeom g, Fr
         block_sync();
     }
     const uint32_t lo = blockIdx.x * chunk, hi = min(ntri, lo + chunk);
-    for (uint32_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
-        const int32_t v = (int32_t)(tri_base + t);
-        const uint32_t yr = __ldg(fb.rows + tri_base + t);
+    for (uint32_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+        const int32_t v = (int32_t)(tri_base + (order ? __ldg(order + p) : p));
+        const uint32_t yr = __ldg(fb.rows + tri_base + p);
         nltree_update(tree, n, (int)(yr & 0xffffu), (int)(yr >> 16), v, kShared);
     }
     if (kShared) {
@@ -220,7 +221,7 @@ newline_kernel(uint32_t ntri, uint32_t tri_base, uint32_t chunk, FrameGeom g, Fr
     }
 }
 
-cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
+cudaError_t launch_newline(uint32_t ntri, const uint32_t *order, uint32_t tri_base, const FrameGeom &g,
                            const FrameBuffers &fb, cudaStream_t s)
 {
     if (ntri == 0 || !g.image) return cudaSuccess;
@@ -231,9 +232,9 @@ cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
         cudaError_t e = cudaFuncSetAttribute(newline_kernel<true>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024);
         if (e != cudaSuccess) return e;
-        newline_kernel<true><<<blocks, 1024, smem, s>>>(ntri, tri_base, chunk, g, fb);
+        newline_kernel<true><<<blocks, 1024, smem, s>>>(ntri, order, tri_base, chunk, g, fb);
     } else {
-        newline_kernel<false><<<blocks, 1024, 0, s>>>(ntri, tri_base, chunk, g, fb);
+        newline_kernel<false><<<blocks, 1024, 0, s>>>(ntri, order, tri_base, chunk, g, fb);
     }
     return cudaGetLastError();
 }

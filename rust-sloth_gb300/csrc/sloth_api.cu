@@ -49,6 +49,7 @@ struct sloth_mesh {
     uint8_t *rgb = nullptr;
     uint32_t nvert = 0, ntri = 0;
     float bbox_max[3] = {0, 0, 0};
+    uint32_t *order = nullptr, *oidx = nullptr;   // setup's order of an indexed mesh (spatial_order)
 };
 
 struct sloth_ctx {
@@ -359,10 +360,11 @@ struct MeshView {
     const uint8_t *rgb;
     uint32_t nvert, ntri;
     int device;
+    const uint32_t *order, *oidx;   // setup's order of an indexed mesh (MeshDev), or null
 };
 MeshView sloth_mesh_view(const sloth_mesh *m)
 {
-    return MeshView{m->x, m->y, m->z, m->idx, m->rgb, m->nvert, m->ntri, m->device};
+    return MeshView{m->x, m->y, m->z, m->idx, m->rgb, m->nvert, m->ntri, m->device, m->order, m->oidx};
 }
 
 // ---------------------------------------------------------------------------------------
@@ -746,6 +748,65 @@ sloth_status sloth_ctx_fragments(sloth_ctx *ctx, uint64_t *fragments)
 // ---------------------------------------------------------------------------------------
 // meshes
 // ---------------------------------------------------------------------------------------
+// Setup's order of an indexed mesh's triangles: ascending Morton code (10 bits an axis,
+// interleaved x, y, z from the lowest bit) of the centroid's place in the box of the
+// finite centroids, ties in index order; a triangle with a non-finite centroid takes code
+// 0.  Triangles next to each other in this order lie close together in space, so the
+// triangles one warp or block sets up land on nearby cells and tiles in any view, and
+// their depth-key reductions and tile counts share cache lines and atomics.  The results
+// do not depend on the order (every output is indexed by the triangle), only the speed.
+static void spatial_order(const float *x, const float *y, const float *z, const uint32_t *idx, uint32_t ntri,
+                          std::vector<uint32_t> &order)
+{
+    const float *v[3] = {x, y, z};
+    std::vector<float> c(3 * (size_t)ntri);
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t t = 0; t < ntri; ++t) {
+        const uint32_t *i = idx + 3 * (size_t)t;
+        for (int a = 0; a < 3; ++a) {
+            const float s = v[a][i[0]] + v[a][i[1]] + v[a][i[2]];
+            c[3 * (size_t)t + a] = s;
+            if (std::isfinite(s)) {
+                lo[a] = std::fmin(lo[a], s);
+                hi[a] = std::fmax(hi[a], s);
+            }
+        }
+    }
+    std::vector<uint32_t> code(ntri);
+    for (uint32_t t = 0; t < ntri; ++t) {
+        uint32_t q[3];
+        bool finite = true;
+        for (int a = 0; a < 3; ++a) {
+            const float s = c[3 * (size_t)t + a];
+            finite = finite && std::isfinite(s);
+            const double f = hi[a] > lo[a] ? ((double)s - lo[a]) / ((double)hi[a] - lo[a]) : 0.0;
+            q[a] = f <= 0.0 ? 0u : f >= 1.0 ? 1023u : (uint32_t)(f * 1024.0);
+        }
+        uint32_t m = 0;
+        if (finite)
+            for (int b = 0; b < 10; ++b)
+                for (int a = 0; a < 3; ++a) m |= ((q[a] >> b) & 1u) << (3 * b + a);
+        code[t] = m;
+    }
+    // stable least-significant-digit radix sort of the 30-bit codes, two digits of 15 bits
+    std::vector<uint32_t> src(ntri), cnt(1u << 15);
+    for (uint32_t t = 0; t < ntri; ++t) src[t] = t;
+    order.assign(ntri, 0u);
+    for (int shift = 0; shift < 30; shift += 15) {
+        std::fill(cnt.begin(), cnt.end(), 0u);
+        for (uint32_t t : src) ++cnt[(code[t] >> shift) & 0x7fffu];
+        uint32_t run = 0;
+        for (uint32_t &k : cnt) {
+            const uint32_t n = k;
+            k = run;
+            run += n;
+        }
+        for (uint32_t t : src) order[cnt[(code[t] >> shift) & 0x7fffu]++] = t;
+        src.swap(order);
+    }
+    order.swap(src);
+}
+
 sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, const float *z,
                                uint32_t nvert, const uint32_t *idx, uint32_t ntri,
                                const uint8_t *rgb, const float *bbox_max, sloth_mesh **out)
@@ -785,6 +846,18 @@ sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, c
     if (!e && ntri) e = cudaMemcpy(m->rgb, rgb, 3 * (size_t)ntri, cudaMemcpyHostToDevice);
     if (!e && idx && ntri) e = cudaMemcpy(m->idx, idx, 3 * (size_t)ntri * sizeof(uint32_t), cudaMemcpyHostToDevice);
     if (e) return cleanup(fail(ctx, SLOTH_ERR_CUDA, "mesh upload failed: %s", cudaGetErrorString(e)));
+    if (idx && ntri > 1) {
+        std::vector<uint32_t> ord;
+        spatial_order(x, y, z, idx, ntri, ord);
+        std::vector<uint32_t> oi(3 * (size_t)ntri);
+        for (uint32_t p = 0; p < ntri; ++p)
+            for (int k = 0; k < 3; ++k) oi[3 * (size_t)p + k] = idx[3 * (size_t)ord[p] + k];
+        if (dalloc(&m->order, ntri) || dalloc(&m->oidx, 3 * (size_t)ntri))
+            return cleanup(fail(ctx, SLOTH_ERR_OUT_OF_MEMORY, "mesh allocation failed"));
+        e = cudaMemcpy(m->order, ord.data(), ntri * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        if (!e) e = cudaMemcpy(m->oidx, oi.data(), oi.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        if (e) return cleanup(fail(ctx, SLOTH_ERR_CUDA, "mesh upload failed: %s", cudaGetErrorString(e)));
+    }
     if (bbox_max) {
         memcpy(m->bbox_max, bbox_max, sizeof m->bbox_max);
     } else {
@@ -817,6 +890,8 @@ void sloth_mesh_destroy(sloth_mesh *m)
     dfree(m->z);
     dfree(m->idx);
     dfree(m->rgb);
+    dfree(m->order);
+    dfree(m->oidx);
     delete m;
 }
 
@@ -891,7 +966,7 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
 
     Mat4 M;
     sloth_mat4_mul(ctx->U, transform, M.m);
-    MeshDev md{mesh->x, mesh->y, mesh->z, mesh->idx, mesh->rgb, mesh->nvert, mesh->ntri};
+    MeshDev md{mesh->x, mesh->y, mesh->z, mesh->idx, mesh->rgb, mesh->nvert, mesh->ntri, mesh->order, mesh->oidx};
     const FrameGeom &g = ctx->g;
     const uint32_t ntiles = (uint32_t)(g.ntx * g.nty);
     cudaStream_t s = ctx->stream;
@@ -905,7 +980,7 @@ sloth_status sloth_draw_mesh(sloth_ctx *ctx, const sloth_mesh *mesh, const float
     // beside the binning kernels
     CU(ctx, cudaEventRecord(ctx->setup_ev, s));
     CU(ctx, cudaStreamWaitEvent(ctx->nl_stream, ctx->setup_ev, 0));
-    CU(ctx, timed(ctx, "newline", [&] { return launch_newline(mesh->ntri, ctx->tri_base, g, ctx->fb, ctx->nl_stream); },
+    CU(ctx, timed(ctx, "newline", [&] { return launch_newline(mesh->ntri, mesh->order, ctx->tri_base, g, ctx->fb, ctx->nl_stream); },
                   ctx->nl_stream));
     CU(ctx, cudaEventRecord(ctx->nl_ev, ctx->nl_stream));
     ctx->nl_pending = true;

@@ -106,11 +106,18 @@ inline uint32_t raster_item_bound(uint32_t ntiles, size_t capacity)
     return (uint32_t)(ntiles + capacity / (kMinSplitEntries / 2) + 1);
 }
 
+// A mesh on the device.  Setup takes an indexed mesh's triangles in a spatial order
+// (order[p]: the triangle at position p; oidx: its three vertex indices, at 3p) so that the
+// triangles of one warp or block lie close together on screen; every output stays indexed
+// by the triangle itself, and the results do not depend on the order.  order and oidx are
+// nullptr for the mesh's own order.
 struct MeshDev {
     const float *x, *y, *z;  // nvert
     const uint32_t *idx;     // 3*ntri or nullptr (soup)
     const uint8_t *rgb;      // 3*ntri
     uint32_t nvert, ntri;
+    const uint32_t *order = nullptr;   // ntri or nullptr
+    const uint32_t *oidx = nullptr;    // 3*ntri or nullptr
 };
 
 struct Mat4 {
@@ -170,7 +177,8 @@ cudaError_t launch_setup(const MeshDev &mesh, const float4 *tv, const Mat4 &M, u
                          const FrameGeom &g, const FrameBuffers &fb, const BinBuffers &bb,
                          cudaStream_t s, int tpb = kDefaultTrianglesPerBlock);
 // newline sentinels (image mode): fold each triangle's row range into the segment tree.
-cudaError_t launch_newline(uint32_t ntri, uint32_t tri_base, const FrameGeom &g,
+// The packed rows are in setup's order of the mesh: order is the mesh's MeshDev::order.
+cudaError_t launch_newline(uint32_t ntri, const uint32_t *order, uint32_t tri_base, const FrameGeom &g,
                            const FrameBuffers &fb, cudaStream_t s);
 cudaError_t launch_bin_count_large(uint32_t tri_base, const FrameGeom &g, const FrameBuffers &fb,
                                    const BinBuffers &bb, cudaStream_t s);
