@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -846,12 +847,20 @@ sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, c
     if (!e && ntri) e = cudaMemcpy(m->rgb, rgb, 3 * (size_t)ntri, cudaMemcpyHostToDevice);
     if (!e && idx && ntri) e = cudaMemcpy(m->idx, idx, 3 * (size_t)ntri * sizeof(uint32_t), cudaMemcpyHostToDevice);
     if (e) return cleanup(fail(ctx, SLOTH_ERR_CUDA, "mesh upload failed: %s", cudaGetErrorString(e)));
+    // setup's spatial order (optional: without host memory for it the mesh keeps its own)
+    std::vector<uint32_t> ord, oi;
     if (idx && ntri > 1) {
-        std::vector<uint32_t> ord;
-        spatial_order(x, y, z, idx, ntri, ord);
-        std::vector<uint32_t> oi(3 * (size_t)ntri);
-        for (uint32_t p = 0; p < ntri; ++p)
-            for (int k = 0; k < 3; ++k) oi[3 * (size_t)p + k] = idx[3 * (size_t)ord[p] + k];
+        try {
+            spatial_order(x, y, z, idx, ntri, ord);
+            oi.resize(3 * (size_t)ntri);
+            for (uint32_t p = 0; p < ntri; ++p)
+                for (int k = 0; k < 3; ++k) oi[3 * (size_t)p + k] = idx[3 * (size_t)ord[p] + k];
+        } catch (const std::bad_alloc &) {
+            ord.clear();
+            oi.clear();
+        }
+    }
+    if (!ord.empty()) {
         if (dalloc(&m->order, ntri) || dalloc(&m->oidx, 3 * (size_t)ntri))
             return cleanup(fail(ctx, SLOTH_ERR_OUT_OF_MEMORY, "mesh allocation failed"));
         e = cudaMemcpy(m->order, ord.data(), ntri * sizeof(uint32_t), cudaMemcpyHostToDevice);

@@ -116,6 +116,23 @@ def test_hostile_soups(ctx, seed):
     assert_same(gpu_render(ctx, meshes, R, w, h, image), ref, f"seed {seed} {w}x{h}")
 
 
+@pytest.mark.parametrize("seed", [3, 8])
+def test_hostile_indexed(ctx, seed):
+    """The hostile soup as an indexed mesh with its faces shuffled: setup's spatial order
+    of an indexed mesh meets huge and non-finite centroids."""
+    rng = np.random.default_rng(2000 + seed)
+    m = dict(hostile_soup(seed, n=1500))
+    nt = m["rgb"].shape[0]
+    perm = rng.permutation(nt)
+    m["idx"] = np.ascontiguousarray(np.arange(3 * nt, dtype=np.uint32).reshape(-1, 3)[perm])
+    m["rgb"] = np.ascontiguousarray(m["rgb"][perm])
+    w, h = int(rng.integers(40, 300)), int(rng.integers(20, 120))
+    R = O.euler_rotation(float(rng.uniform(-math.pi, math.pi)), 0.3, 0.1)
+    for image in (False, True):
+        ref = oracle_render([m], R, w, h, image)
+        assert_same(gpu_render(ctx, [m], R, w, h, image), ref, f"seed {seed} {w}x{h}")
+
+
 @pytest.mark.parametrize("w,h", [(3840 // 8, 2160 // 8), (481, 271)])
 def test_scaled_config2_soup(ctx, w, h):
     """Config-2 soup statistics (small N(0,0.02) triangles + large ones) at reduced size."""
