@@ -341,11 +341,13 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) batch_raster
 }
 
 // blocks[i] = (frame, first cell): runs of kBatchRun frame cells per lane (resolve_run),
-// written with one store per buffer when the frame's outputs are aligned.
+// written with one store per buffer when the frame's outputs are aligned.  Four resident
+// blocks per SM (64 registers, no spills): the winners' record loads are latency-bound, and
+// the fourth block's loads in flight took config 3 from 3.33 to 3.22 ms.
 constexpr int kBatchRun = 2;
 static_assert(kBatchResolveChunk % (kBatchRun * 256) == 0, "whole runs, the same trip count in every warp");
 
-__global__ void __launch_bounds__(256) batch_resolve_kernel(BatchDev b, const int2 *__restrict__ blocks)
+__global__ void __launch_bounds__(256, 4) batch_resolve_kernel(BatchDev b, const int2 *__restrict__ blocks)
 {
     // the frame's descriptor in shared memory: read there, its fields are not reloaded
     // from global memory after each of the block's output stores
