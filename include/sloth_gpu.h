@@ -208,7 +208,10 @@ sloth_status sloth_tile_shape(int shape, uint32_t *cells, uint32_t *rows);
  * (triangle t uses vertices 3t, 3t+1, 3t+2; then nvert must be 3*ntri).  rgb: 3*ntri
  * face colours (Triangle.color).  bbox_max: the SimpleMesh bounding_box.max (x,y,z) that
  * Context::update folds, or NULL to use the loader rule of OBJ meshes
- * (src/geometry.rs:86-89,128-135: a box grown from the origin). */
+ * (src/geometry.rs:86-89,128-135: a box grown from the origin).  An indexed mesh also
+ * gets the order in which setup takes its triangles (a Morton order of their centroids,
+ * sorted on the host here, 16 more device bytes a triangle); draws still follow the
+ * mesh's own triangle order, which the results depend on, not that one. */
 sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, const float *z,
                                uint32_t nvert, const uint32_t *idx, uint32_t ntri,
                                const uint8_t *rgb, const float *bbox_max, sloth_mesh **out);
