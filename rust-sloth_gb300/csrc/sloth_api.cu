@@ -860,9 +860,14 @@ sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, c
             oi.clear();
         }
     }
+    if (!ord.empty() && (dalloc(&m->order, ntri) || dalloc(&m->oidx, 3 * (size_t)ntri))) {
+        // no device memory for it: the mesh keeps its own order
+        dfree(m->order);
+        dfree(m->oidx);
+        cudaGetLastError();
+        ord.clear();
+    }
     if (!ord.empty()) {
-        if (dalloc(&m->order, ntri) || dalloc(&m->oidx, 3 * (size_t)ntri))
-            return cleanup(fail(ctx, SLOTH_ERR_OUT_OF_MEMORY, "mesh allocation failed"));
         e = cudaMemcpy(m->order, ord.data(), ntri * sizeof(uint32_t), cudaMemcpyHostToDevice);
         if (!e) e = cudaMemcpy(m->oidx, oi.data(), oi.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
         if (e) return cleanup(fail(ctx, SLOTH_ERR_CUDA, "mesh upload failed: %s", cudaGetErrorString(e)));
