@@ -793,7 +793,8 @@ CONFIG5_LAPLACIAN = 1e5      # weight of sum(|L p|^2), uniform mesh Laplacian on
 def run_config5(torch, stream, device, args, steps=200):
     """Inverse rendering: Adam on vertex positions and colours through the differentiable
     path (loss = sum of squared image differences + a uniform-Laplacian smoothness term on
-    the positions), visibility stored (it fits the 1 GB budget) and recomputed."""
+    the positions), visibility stored (it fits the 1 GB budget) and recomputed; and, not
+    timed, the same fit with the image term alone, its RMSE every 20 steps."""
     import diff_render as DR
     import sloth_gpu as S
     import workloads as W
@@ -816,7 +817,7 @@ def run_config5(torch, stream, device, args, steps=200):
            "loss": f"sum((rgb - target)^2) + {CONFIG5_LAPLACIAN:g} * sum(|L p|^2), L the uniform mesh Laplacian",
            "rmse": "over every depth cell and channel of the 64 views (background included)"}
 
-    def optimise(sv, nsteps, timed):
+    def optimise(sv, nsteps, timed, lap_w=CONFIG5_LAPLACIAN):
         pos = torch.from_numpy(p0).to(dev).requires_grad_(True)
         col = torch.full((p0.shape[0], 3), 0.5, dtype=torch.float32, device=dev, requires_grad=True)
         opt = torch.optim.Adam([pos, col], lr=1e-2)
@@ -826,18 +827,25 @@ def run_config5(torch, stream, device, args, steps=200):
                 return float(torch.sqrt(((DR.shade_views(pos, col, light, sv) - target) ** 2).mean()))
 
         r0 = rmse()
+        trace = []
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         a.record(stream)
-        for _ in range(nsteps):
+        for i in range(nsteps):
             opt.zero_grad(set_to_none=True)
-            loss = ((DR.shade_views(pos, col, light, sv) - target) ** 2).sum() + CONFIG5_LAPLACIAN * (lap(pos) ** 2).sum()
+            loss = ((DR.shade_views(pos, col, light, sv) - target) ** 2).sum()
+            if lap_w:
+                loss = loss + lap_w * (lap(pos) ** 2).sum()
             loss.backward()
             opt.step()
+            if not timed and (i + 1) % 20 == 0:
+                trace.append(round(rmse(), 5))
         b.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        if not timed:
+            return {"rmse_initial": r0, "rmse_every_20_steps": trace, "rmse_final": rmse()}
         return {"steps_per_s": nsteps / wall, "device_ms_per_step": a.elapsed_time(b) / nsteps,
                 "rmse_initial": r0, "rmse_final": rmse()}
 
@@ -847,6 +855,12 @@ def run_config5(torch, stream, device, args, steps=200):
         r = optimise(sv, steps, True)
         r["visibility_bytes"] = sv.ncells * DR.ShadedViews.VIS_BYTES_PER_CELL if sv.store_visibility else 0
         out["stored" if sv.store_visibility else "recomputed"] = r
+        if sv.store_visibility:
+            # the loss with the image term alone, as the workload states it (not timed): with
+            # visibility held fixed the positions get no silhouette gradient and drift
+            nr = optimise(sv, steps, False, lap_w=0.0)
+            out["image_term_only"] = {"loss": "sum((rgb - target)^2)", **nr,
+                                      "rmse_min": min([nr["rmse_initial"]] + nr["rmse_every_20_steps"])}
         sv.close()
     torch.cuda.synchronize()
     ctx.close()
