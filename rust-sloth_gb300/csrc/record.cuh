@@ -72,10 +72,11 @@ __device__ __forceinline__ int sat_hi(float f)
 }
 
 // Stores a record.  A triangle with no tile (culled, empty sample range) only ever has its
-// sample range read -- by the newline and fill kernels, which stop there -- so only that
-// row is written, with zeros in row 5 beside it (store_row4: a whole 32-byte sector, which
-// the memory writes back without reading it first).  A direct triangle (direct.cuh) is never binned nor rasterized again:
-// only the rows the resolve (0-1, 5) and the newline and fill kernels (4) read are written.
+// sample range read -- by a context's overflow fold and the no-allocation raster, which
+// stop there -- so only that row is written, with zeros in row 5 beside it (store_row4: a
+// whole 32-byte sector, which the memory writes back without reading it first).  A direct
+// triangle (direct.cuh) is never binned nor rasterized again: only the rows the resolve
+// (0-1, 5) and a context's overflow fold (4) read are written.
 __device__ __forceinline__ void store_record(TriRecord *dst, const TriRecord &r, uint32_t ntiles, bool direct = false)
 {
     const int4 *src = reinterpret_cast<const int4 *>(&r);
