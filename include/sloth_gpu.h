@@ -79,6 +79,17 @@ float sloth_scene_extent(const float *bbox_max, uint32_t nmesh);
  * context and a scene extent.  out: row-major 4x4. */
 void sloth_viewport_transform(uint16_t width, uint16_t height, float extent, float out[16]);
 
+/* The order in which setup takes an indexed mesh's triangles (host only, no device
+ * needed): order[p] is the triangle at position p, by ascending Morton code (10 bits an
+ * axis, x in the lowest bit) of its centroid's place in the box of the finite centroids,
+ * ties in index order, a non-finite centroid taking code 0.  sloth_mesh_create makes it
+ * for every indexed mesh; the results of a draw do not depend on it.  x, y, z: nvert
+ * vertex positions; idx: 3*ntri indices; order: ntri outputs.  SLOTH_ERR_INVALID_ARGUMENT
+ * for NULL arrays or an index not below nvert, SLOTH_ERR_OUT_OF_MEMORY without host
+ * memory for the sort. */
+sloth_status sloth_spatial_order(const float *x, const float *y, const float *z, uint32_t nvert, const uint32_t *idx,
+                                 uint32_t ntri, uint32_t *order);
+
 /* ---- context (src/context.rs:12-49) ------------------------------------------------- */
 
 /* Create a context on CUDA device `device`.  `stream` is a cudaStream_t to order all

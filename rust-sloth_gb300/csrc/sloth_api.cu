@@ -808,6 +808,22 @@ static void spatial_order(const float *x, const float *y, const float *z, const 
     order.swap(src);
 }
 
+sloth_status sloth_spatial_order(const float *x, const float *y, const float *z, uint32_t nvert, const uint32_t *idx,
+                                 uint32_t ntri, uint32_t *order)
+{
+    if (ntri && (!x || !y || !z || !idx || !order)) return SLOTH_ERR_INVALID_ARGUMENT;
+    for (uint64_t i = 0; i < 3ull * ntri; ++i)
+        if (idx[i] >= nvert) return SLOTH_ERR_INVALID_ARGUMENT;
+    try {
+        std::vector<uint32_t> ord;
+        spatial_order(x, y, z, idx, ntri, ord);
+        std::copy(ord.begin(), ord.end(), order);
+    } catch (const std::bad_alloc &) {
+        return SLOTH_ERR_OUT_OF_MEMORY;
+    }
+    return SLOTH_OK;
+}
+
 sloth_status sloth_mesh_create(sloth_ctx *ctx, const float *x, const float *y, const float *z,
                                uint32_t nvert, const uint32_t *idx, uint32_t ntri,
                                const uint8_t *rgb, const float *bbox_max, sloth_mesh **out)

@@ -43,6 +43,7 @@ SIGNATURES = {
     "sloth_mat4_mul": (None, [_f32p, _f32p, _f32p]),
     "sloth_scene_extent": (C.c_float, [_f32p, C.c_uint32]),
     "sloth_viewport_transform": (None, [C.c_uint16, C.c_uint16, C.c_float, _f32p]),
+    "sloth_spatial_order": (C.c_int, [_f32p, _f32p, _f32p, C.c_uint32, _u32p, C.c_uint32, _u32p]),
     "sloth_ctx_create": (C.c_int, [C.POINTER(_vp), C.c_int, _vp]),
     "sloth_ctx_destroy": (None, [_vp]),
     "sloth_ctx_last_error": (C.c_char_p, [_vp]),
@@ -148,6 +149,21 @@ def mat4_mul(a, b) -> np.ndarray:
 def scene_extent(bbox_max) -> float:
     b = np.ascontiguousarray(np.asarray(bbox_max, np.float32).reshape(-1, 3))
     return float(load_library().sloth_scene_extent(_ptr(b, C.c_float), b.shape[0]))
+
+
+def spatial_order(x, y, z, idx) -> np.ndarray:
+    """The order in which setup takes an indexed mesh's triangles (sloth_spatial_order)."""
+    x, y, z = (np.ascontiguousarray(a, np.float32) for a in (x, y, z))
+    idx = np.ascontiguousarray(idx, np.uint32).reshape(-1)
+    ntri = idx.size // 3
+    out = np.zeros(max(ntri, 1), np.uint32)
+    if not (x.size == y.size == z.size):
+        raise ValueError("x, y and z differ in length")
+    st = load_library().sloth_spatial_order(_ptr(x, C.c_float), _ptr(y, C.c_float), _ptr(z, C.c_float), x.size,
+                                            _ptr(idx, C.c_uint32), ntri, _ptr(out, C.c_uint32))
+    if st != 0:
+        raise SlothError(st, "sloth_spatial_order")
+    return out[:ntri]
 
 
 def viewport_transform(width: int, height: int, extent: float) -> np.ndarray:
