@@ -126,6 +126,47 @@ def test_batch_entry_overflow_replans(ctx):
     b.close()
 
 
+def test_batch_exact_across_setting_changes(ctx):
+    """One batch through graph replays, new transforms, the direct path switched off and
+    on, a tile-shape change and an entry overflow with the direct path on, on even- and
+    odd-width frames: every frame exact after every render (the keys the direct folds
+    need are cleared at the right renders, the graph is captured again when it must)."""
+    meshes, dev, frames = mixed_frames(ctx)
+    frames = frames[:10]
+    b = S.Batch(ctx, frames)
+    rng = np.random.default_rng(17)
+
+    def new_transforms():
+        mats = []
+        for f in frames:
+            R = O.euler_rotation(*W.cli_rotation(yaw=float(rng.uniform(0, 6.28))))
+            f["R"] = R
+            mats += [R] * len(f["draws"])
+        b.set_transforms(np.stack(mats))
+
+    steps = [("direct 64", lambda: b.set_direct_samples(64)), ("replay", None), ("replay", None),
+             ("transforms", new_transforms), ("direct 0", lambda: b.set_direct_samples(0)),
+             ("direct 16", lambda: b.set_direct_samples(16)), ("replay", None),
+             ("shape 1", lambda: b.set_tile_shape(1)), ("replay", None), ("transforms", new_transforms)]
+    for name, change in steps:
+        if change:
+            change()
+        b.render()
+        check_frames(b, meshes, frames, name)
+    # a transform that overflows the entry buffer, with the direct path on
+    big = np.diag([4.0, 4.0, 4.0, 1.0]).astype(np.float32)
+    mats = []
+    for f in frames:
+        f["R"] = O.mat4_mul(f["R"], big)
+        mats += [f["R"]] * len(f["draws"])
+    b.set_transforms(np.stack(mats))
+    b.render()
+    check_frames(b, meshes, frames, "overflow")
+    b.render()
+    check_frames(b, meshes, frames, "after the overflow")
+    b.close()
+
+
 @pytest.mark.parametrize("direct,tpb", [(0, 128), (16, 4096), (4, 256)])
 def test_context_tuning_settings(ctx, direct, tpb):
     """Every value of the autotuner's other dimensions renders the same frame."""
